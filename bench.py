@@ -1,0 +1,369 @@
+"""Benchmark of the per-step fluid solver (cell-updates/s, % of HBM roofline).
+
+Default workload: 2048x2048 FP32, vorticity confinement 0.35, viscosity 0, 80
+Jacobi sweeps, 12 circular obstacles re-added every step, 16 Gaussian splats
+per step on velocity and density, density advection, dt = 1/60.  A "step" is
+one frame: obstacles, forcing, FluidSimulator.update, SmoothParticlesArea.update.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl natrix|reference]
+                  [--workload large|small]
+
+One JSON line on rank 0.  `value` is timed with CUDA events on the launching
+stream with the fields resident on the device (the per-step forcing records,
+~1.5 KB, go through the API's pinned staging as they would for any caller).
+`e2e` adds, every step, a device->host read of the density frame into pinned
+host memory through the C ABI and the wait for it.  `roofline` is the Jacobi
+phase (the dominant kernel), timed live with CUDA events around its launches.
+`cpu_baseline` times the CPU oracle (float32, all host threads) on a bounded
+sample of the same workload.  `--impl reference` times that CPU
+implementation alone, as the reference arm.
+
+Multi-GPU: the path does not shard (one simulation per GPU); with N ranks each
+rank advances its own replica ("replicas only", weak scaling) and `value` is
+the total over ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+from natrix_gb300 import workloads as wl  # noqa: E402
+
+# Algorithmic bytes per cell (float2 velocity 8 B, float scalars 4 B, uint8
+# obstacle mask and neighbour flags 1 B; each kernel reads its inputs once and
+# writes its outputs once).
+BYTES = {
+    "forcing": 24,           # velocity r/w 16 + density r/w 8
+    "advect": 17,            # velocity in 8, mask 1, velocity out 8
+    "density_advect": 17,    # density in 4, velocity 8, mask 1, density out 4
+    "vorticity_calc": 12,    # velocity 8, vorticity out 4
+    "vorticity_apply": 20,   # velocity 8, vorticity 4, velocity out 8
+    "divergence": 13,        # velocity 8, mask 1, divergence out 4
+    "jacobi_sweep": 13,      # pressure 4, divergence 4, flags 1, pressure out 4
+    "subtract_gradient": 21, # velocity 8, pressure 4, flags 1, velocity out 8
+}
+
+
+def step_bytes_per_cell(spec: wl.Workload) -> int:
+    b = BYTES["forcing"] + BYTES["advect"] + BYTES["density_advect"] + BYTES["divergence"]
+    b += BYTES["subtract_gradient"] + BYTES["jacobi_sweep"] * spec.iterations
+    if spec.vorticity > 0:
+        b += BYTES["vorticity_calc"] + BYTES["vorticity_apply"]
+    return b
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = []
+        with open(self.path) as f:
+            for r in csv.reader(f):
+                if len(r) >= 9:
+                    rows.append([c.strip() for c in r])
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def make_spec(name: str) -> wl.Workload:
+    return {"large": wl.LARGE_2048, "small": wl.SMALL_256}[name]
+
+
+def workload_config(spec: wl.Workload, extra=None):
+    cfg = {"workload": spec.name, "grid": [spec.width, spec.height],
+           "jacobi_sweeps": spec.iterations, "vorticity": spec.vorticity,
+           "viscosity": spec.viscosity, "dissipation": spec.dissipation, "speed": spec.speed,
+           "dt": spec.dt, "splats_per_step": spec.splats_per_step,
+           "obstacles": spec.n_obstacles, "density_grid": [spec.width, spec.height],
+           "dtype": "fp32", "l2": "working set per step > L2 (no explicit flush)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# ------------------------------------------------------------------ CPU legs
+def cpu_run(spec: wl.Workload, steps: int, warmup: int, seed: int = 0):
+    """Time the float32 CPU oracle (OpenMP, all host threads) on `steps`
+    frames after `warmup` frames; returns (seconds per step, threads)."""
+    from oracle import oracle as O
+
+    f = O.OracleFluid(spec.width, spec.height, np.float32)
+    d = O.OracleDensity(spec.width, spec.height, f)
+    f.iterations, f.vorticity, f.viscosity = spec.iterations, spec.vorticity, spec.viscosity
+    f.speed, f.dissipation = spec.speed, spec.dissipation
+    d.speed, d.dissipation = spec.speed, spec.dissipation
+    obst = wl.workload_obstacles(seed, spec)
+    times = []
+    for i in range(warmup + steps):
+        splats = wl.step_forcing(seed, i, spec)
+        t0 = time.perf_counter()
+        for o in obst:
+            f.add_circle_obstacle((float(o[0]), float(o[1])), float(o[2]))
+        f.add_splats(splats, d)
+        f.update(spec.dt)
+        d.update(spec.dt)
+        if i >= warmup:
+            times.append(time.perf_counter() - t0)
+    return float(np.mean(times)), O.num_threads()
+
+
+def cpu_sample_steps(spec: wl.Workload) -> int:
+    return 3 if spec.width >= 1024 else 50
+
+
+def run_reference(args, spec):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cells = spec.width * spec.height
+    steps = max(1, min(args.steps, cpu_sample_steps(spec)))
+    warm = max(1, min(args.warmup, 1))
+    sec, threads = cpu_run(spec, steps, warm)
+    value = cells / sec
+    sample = f"{steps} timed frames after {warm} warm-up of the {spec.width}x{spec.height} workload"
+    line = {
+        "impl": "reference", "metric": "cell-updates/s", "value": value,
+        "unit": "cell-updates/s", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded splats and discs)",
+        "config": workload_config(spec),
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": ("the reference's own path is bgfx compute shaders that need a graphics "
+                 "stack (unavailable on this box); its CPU stand-in is the C oracle, a "
+                 "float32 restatement of those shaders pinned bit-for-bit to them"),
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU leg
+def run_natrix(args, spec):
+    import torch
+    import torch.distributed as dist
+
+    from natrix_gb300 import FluidSimulator, SmoothParticlesArea, _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    W, H = spec.width, spec.height
+    cells = W * H
+    sim = FluidSimulator(W, H)
+    den = SmoothParticlesArea(W, H, sim)
+    sim.iterations, sim.vorticity, sim.viscosity = spec.iterations, spec.vorticity, spec.viscosity
+    sim.speed, sim.dissipation = spec.speed, spec.dissipation
+    den.speed, den.dissipation = spec.speed, spec.dissipation
+    seed = rank
+    obst = wl.workload_obstacles(seed, spec)
+    total = args.warmup + 2 * args.steps
+    forcing = [wl.step_forcing(seed, i, spec) for i in range(total)]
+    stream = torch.cuda.current_stream()
+
+    def frame(i):
+        for o in obst:
+            sim.add_circle_obstacle((float(o[0]), float(o[1])), float(o[2]))
+        sim.add_splats(forcing[i], den)
+        sim.update(spec.dt)
+        den.update(spec.dt)
+
+    for i in range(args.warmup):
+        frame(i)
+    sim.sync()
+    torch.cuda.synchronize()
+
+    lib = _lib.load()
+    stats = _lib.Stats()
+    lib.natrix_get_stats(sim.handle, stats, 1)
+    lib.natrix_set_timing(sim.handle, 1)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for i in range(args.warmup, args.warmup + args.steps):
+            frame(i)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    lib.natrix_set_timing(sim.handle, 0)
+    ms = ev0.elapsed_time(ev1)
+    _lib.check(lib.natrix_get_stats(sim.handle, stats, 1))
+    sim.sync()
+    launches = int(stats.kernel_launches)
+
+    # e2e: the same frames through the C ABI with a device->host read of
+    # every frame's density into pinned host memory, waited on each step
+    host = torch.empty((H, W), dtype=torch.float32).pin_memory()
+    hp = host.data_ptr()
+    import ctypes
+
+    hptr = ctypes.c_void_p(hp)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.warmup + args.steps, total):
+        frame(i)
+        _lib.check(lib.natrix_density_download(den.handle, hptr, sptr))
+        stream.synchronize()
+    t_e2e = time.perf_counter() - t0
+    barrier()
+    sim.sync()
+
+    ms_t = torch.tensor([ms, t_e2e * 1e3], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms, ms_e2e = float(ms_t[0]), float(ms_t[1])
+    value = cells * args.steps * world / (ms / 1e3)
+    e2e_value = cells * args.steps * world / (ms_e2e / 1e3)
+
+    peak, peak_kind = load_peaks()
+    step_b = step_bytes_per_cell(spec)
+    jl = max(int(stats.timed_launches), 1)
+    launch_ms = stats.jacobi_ms / jl
+    sweeps_per_launch = stats.timed_sweeps / jl
+    alg_bytes = BYTES["jacobi_sweep"] * cells * sweeps_per_launch
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    traffic = load_traffic(spec)
+
+    if rank == 0:
+        # per-frame host->device bytes: splat records for velocity and density,
+        # obstacle shapes, two step-parameter blocks (sizes of the C structs)
+        h2d = 32 * spec.splats_per_step * 2 + 32 * spec.n_obstacles + 48 * 2
+        cpu = None
+        if not args.no_cpu:
+            csec, threads = cpu_run(spec, cpu_sample_steps(spec), 1)
+            cpu = {"value": cells / csec, "unit": "cell-updates/s", "cores": threads,
+                   "kind": "port",
+                   "sample": f"{cpu_sample_steps(spec)} frames after 1 warm-up, "
+                             f"{W}x{H}, float32 C oracle (OpenMP)"}
+        line = {
+            "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Gaussian splats and non-overlapping discs)",
+            "config": workload_config(spec, {"parallelism": f"replicas{world}"}),
+            "hbm_roofline_model": {
+                "bytes_per_cell_step": step_b,
+                "achieved_gbs": value * step_b / 1e9,
+                "frac": value * step_b / 1e9 / peak,
+                "peak_gbs": peak, "peak_kind": peak_kind},
+            "roofline": {"kernel": "jacobi (temporally blocked, TMA tiles)", "bound": "hbm",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_kind": peak_kind,
+                         "launch_ms": launch_ms, "sweeps_per_launch": sweeps_per_launch,
+                         "bytes_model": "13 B per cell per sweep"},
+            "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": cells * 4},
+            "gpu_launches": launches,
+            "gpu_launches_per_step": launches / args.steps,
+            "clocks": clocks.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    den.destroy()
+    sim.destroy()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def load_traffic(spec):
+    """DRAM bytes per Jacobi launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get(spec.name)
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["natrix", "reference"], default="natrix")
+    ap.add_argument("--workload", choices=["large", "small"], default="large")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "natrix":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    spec = make_spec(args.workload)
+    if args.impl == "reference":
+        run_reference(args, spec)
+    else:
+        run_natrix(args, spec)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,189 @@
+/* natrix_gb300 — C ABI of the GB300 (sm_103a) fluid solver.
+ *
+ * Drop-in for the per-step solver behind natrix.core's FluidSimulator
+ * (natrix/core/fluid_simulator.py) and the demo's SmoothParticlesArea
+ * (demo/smooth_particles_area.py).  Each entry point names the reference
+ * member it replaces.
+ *
+ * Conventions
+ *  - Every entry point returns 0 on success or a negative NATRIX_E* code;
+ *    natrix_last_error() gives the message of the calling thread's last error.
+ *  - The library owns the device memory of each handle (cudaMalloc at
+ *    creation, cudaFree at destroy), on the device current at creation.
+ *  - `stream` arguments are cudaStream_t values passed as void*; NULL is the
+ *    legacy default stream.  Work on one handle must be issued on one stream
+ *    (or externally ordered); separate handles are independent.
+ *  - Not thread-safe per handle.
+ *  - Mutating calls (add_*, step) are no-ops while the `simulate` parameter
+ *    is 0, as in the reference.  add_* calls are queued on the host and
+ *    applied by one fused kernel before the next step or field access.
+ *  - Device fields are row-major with a row pitch in elements
+ *    (natrix_field); pitch >= width and rows are 128-byte aligned.
+ */
+#ifndef NATRIX_GB300_NATRIX_H
+#define NATRIX_GB300_NATRIX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NATRIX_OK 0
+#define NATRIX_EINVAL -1  /* bad argument (the reference raises ValueError) */
+#define NATRIX_ECUDA -2   /* a CUDA runtime call failed */
+#define NATRIX_ENOMEM -3  /* device or host allocation failed */
+#define NATRIX_EDEVICE -4 /* a kernel reported an error status (bounded wait) */
+#define NATRIX_ERANGE -5  /* size beyond a documented maximum */
+
+typedef struct natrix_sim natrix_sim;
+typedef struct natrix_density natrix_density;
+
+/* Simulator parameters; defaults as natrix/core/fluid_simulator.py:28-35. */
+typedef struct natrix_params {
+    float speed;       /* > 0, default 500   (FluidSimulator.speed, :58-66)       */
+    int32_t iterations; /* > 0, default 50   (FluidSimulator.iterations, :68-76)  */
+    float dissipation; /* > 0, default 1.0   (FluidSimulator.dissipation, :78-86) */
+    float vorticity;   /* >= 0, default 0    (FluidSimulator.vorticity, :88-96)   */
+    float viscosity;   /* >= 0, default 0.1  (FluidSimulator.viscosity, :98-111)  */
+    int32_t has_borders; /* default 1        (FluidSimulator.has_borders, :34)    */
+    int32_t simulate;  /* default 1          (FluidSimulator.simulate, :35)       */
+    int32_t sweeps_per_launch; /* Jacobi sweeps fused per launch (temporal
+                                  blocking); 0 = library default */
+} natrix_params;
+
+/* Fields of a simulator (natrix_field / natrix_upload / natrix_download). */
+enum natrix_field_id {
+    NATRIX_FIELD_VELOCITY = 0,   /* float2 [H][pitch]; FluidSimulator.get_velocity_buffer, :113-114 */
+    NATRIX_FIELD_PRESSURE = 1,   /* float  [H][pitch]; pressure after the last step's sweeps */
+    NATRIX_FIELD_DIVERGENCE = 2, /* float  [H][pitch] */
+    NATRIX_FIELD_VORTICITY = 3,  /* float  [H][pitch] */
+    NATRIX_FIELD_OBSTACLES = 4   /* uint8  [H][pitch]; bit0 = obstacle (x), bit1 = static triangle (y) */
+};
+
+/* Number of floats per splat record passed to natrix_add_splats. */
+#define NATRIX_SPLAT_FLOATS 6
+
+/* Create a width x height simulator (FluidSimulator.__init__,
+ * natrix/core/fluid_simulator.py:37-48; the bgfx vertex layout has no
+ * counterpart).  Fields start at zero, parameters at their defaults. */
+int natrix_create(int32_t width, int32_t height, natrix_sim** out);
+
+/* Free every device buffer of the handle (FluidSimulator.destroy, :476-515). */
+int natrix_destroy(natrix_sim* sim);
+
+/* Set / get all parameters.  Validation follows the property setters of
+ * natrix/core/fluid_simulator.py:58-111: speed, iterations and dissipation
+ * must be > 0, vorticity and viscosity >= 0, else NATRIX_EINVAL. */
+int natrix_set_params(natrix_sim* sim, const natrix_params* params);
+int natrix_get_params(const natrix_sim* sim, natrix_params* params);
+
+/* Cone velocity splat at a normalised position with radius in cells, then
+ * the clamp of every cell to [-1, 1] (FluidSimulator.add_velocity, :116-131;
+ * shader.AddVelocity.comp). */
+int natrix_add_velocity(natrix_sim* sim, float px, float py, float vx, float vy, float radius);
+
+/* Obstacle disc (FluidSimulator.add_circle_obstacle, :135-153;
+ * shader.AddCircleObstacle.comp). */
+int natrix_add_circle_obstacle(natrix_sim* sim, float px, float py, float radius,
+                               int32_t is_static);
+
+/* Obstacle triangle in normalised coordinates (FluidSimulator.add_triangle_obstacle,
+ * :156-172; shader.AddTriangleObstacle.comp). */
+int natrix_add_triangle_obstacle(natrix_sim* sim, float x1, float y1, float x2, float y2,
+                                 float x3, float y3, int32_t is_static);
+
+/* Gaussian splat forcing of velocity and, when `density` is not NULL, of
+ * that density grid: `n` host records of NATRIX_SPLAT_FLOATS floats
+ * {px, py, radius_cells, vx, vy, density}.  No reference counterpart: it is
+ * the forcing of the benchmark workloads (weight exp(-d^2/r^2) inside 3r,
+ * velocity clamped to [-1, 1] after each splat, density to [0, 255]). */
+int natrix_add_splats(natrix_sim* sim, natrix_density* density, const float* splats,
+                      int32_t n);
+
+/* Advance one step (FluidSimulator.update, :174-280): boundaries, advection,
+ * vorticity confinement, viscosity, divergence, `iterations` Jacobi sweeps
+ * from zero, gradient subtraction, obstacle reset. */
+int natrix_step(natrix_sim* sim, float dt, void* stream);
+
+/* Device pointer and row pitch (elements) of a field's current buffer.  The
+ * pointer can change after natrix_step; query it again after each step. */
+int natrix_field(natrix_sim* sim, int32_t field, void** dev_ptr, int64_t* pitch_elems);
+
+/* Copy a field between a dense host array (H*W elements, rows of W) and the
+ * device (stream-ordered; the host buffer should be pinned for async copies,
+ * the call returns after enqueueing). */
+int natrix_upload(natrix_sim* sim, int32_t field, const void* host, void* stream);
+int natrix_download(natrix_sim* sim, int32_t field, void* host, void* stream);
+
+/* Residual of the pressure system the sweeps iterate, over fluid cells:
+ * out = {n, sum r, sum r^2, sum b, sum b^2} with r = b - (sum p_nbr - 4 p)
+ * (same neighbour rule as shader.Poisson.comp).  Synchronises `stream`.
+ * No reference counterpart. */
+int natrix_residual(natrix_sim* sim, double out[5], void* stream);
+
+/* Run `sweeps` more Jacobi sweeps on the current pressure (no reset), with
+ * the divergence and obstacles of the last step.  No reference counterpart
+ * (used for residual-driven solves and warm starts). */
+int natrix_jacobi(natrix_sim* sim, int32_t sweeps, void* stream);
+
+/* Wait for the handle's work and return NATRIX_EDEVICE if a kernel recorded
+ * an error status (bounded waits that ran out).  Clears the status. */
+int natrix_sync(natrix_sim* sim, void* stream);
+
+/* --- density grid: SmoothParticlesArea (demo/smooth_particles_area.py) --- */
+
+/* Density grid of its own size, advected by `fluid`'s velocity
+ * (SmoothParticlesArea.__init__, :28-46). */
+int natrix_density_create(natrix_sim* fluid, int32_t width, int32_t height,
+                          natrix_density** out);
+int natrix_density_destroy(natrix_density* d);
+
+/* speed > 0 and dissipation > 0 (SmoothParticlesArea.speed / .dissipation,
+ * :48-68); simulate as the reference's flag (:26). */
+int natrix_density_set_params(natrix_density* d, float speed, float dissipation,
+                              int32_t simulate);
+
+/* Cone density splat, clamped to [0, 255] inside the radius
+ * (SmoothParticlesArea.add_particles, :70-83; shader.AddParticle.comp).
+ * Rows the reference's dispatch does not reach (y >= 16*ceil(W/16)) are
+ * left unchanged. */
+int natrix_density_add(natrix_density* d, float px, float py, float radius, float strength);
+
+/* Advect the density by the fluid's current velocity
+ * (SmoothParticlesArea.update, :85-104; shader.AdvectParticle.comp). */
+int natrix_density_step(natrix_density* d, float dt, void* stream);
+
+int natrix_density_field(natrix_density* d, void** dev_ptr, int64_t* pitch_elems);
+int natrix_density_upload(natrix_density* d, const float* host, void* stream);
+int natrix_density_download(natrix_density* d, float* host, void* stream);
+
+/* Counters of one handle (and the density grids attached to it). */
+typedef struct natrix_stats {
+    int64_t kernel_launches; /* kernels this library launched for the handle */
+    int64_t jacobi_launches; /* of which temporally blocked Jacobi launches */
+    int64_t jacobi_sweeps;   /* Jacobi sweeps those launches ran */
+    int64_t timed_phases;    /* Jacobi phases bracketed by CUDA events */
+    int64_t timed_launches;  /* Jacobi launches inside the timed phases */
+    int64_t timed_sweeps;    /* sweeps inside the timed phases */
+    double jacobi_ms;        /* device time of the timed phases (CUDA events) */
+} natrix_stats;
+
+/* Bracket the Jacobi phase of every following step with CUDA events on the
+ * step's stream (enable = 1) or stop (0).  No reference counterpart. */
+int natrix_set_timing(natrix_sim* sim, int32_t enable);
+
+/* Read the counters (waits for the timed events); reset = 1 zeroes them. */
+int natrix_get_stats(natrix_sim* sim, natrix_stats* out, int32_t reset);
+
+/* Message of the calling thread's last error ("" if none). */
+const char* natrix_last_error(void);
+
+/* Library version string. */
+const char* natrix_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NATRIX_GB300_NATRIX_H */

@@ -1,0 +1,101 @@
+// Device-side helpers shared by the solver kernels.
+//
+// Arithmetic contract: the solver translation units are compiled with
+// -fmad=false and IEEE division / square root (nvcc's defaults
+// -prec-div=true -prec-sqrt=true), so each + - * / and sqrtf below rounds
+// once, in the order written.  The order follows the reference shader text
+// (natrix/core/shaders/originals/*.comp), which makes the FP32 results equal,
+// bit for bit, to the oracle's float instantiation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace natrix {
+
+// 2-D field geometry: width, height and row pitch in elements.
+struct Grid {
+    int W, H, P;
+};
+
+__device__ __forceinline__ float clampf(float v, float lo, float hi) {
+    // GLSL clamp = min(max(x, lo), hi), in the form the oracle uses
+    float m = v > lo ? v : lo;
+    return m < hi ? m : hi;
+}
+
+// GLSL mix, HLSL lerp form: a + t*(b - a)
+__device__ __forceinline__ float mixf(float a, float b, float t) { return a + t * (b - a); }
+
+// Bilinear sampler of shader.AdvectVelocity.comp:38-48 (and GetVelocity in
+// demo/shaders/shader.AdvectParticle.comp:21-35): corners from ceil/floor of
+// the sample position clamped to the grid, the fractional delta NOT clamped
+// (so positions outside the grid extrapolate linearly, as the reference does).
+struct Corners {
+    int lo_x, lo_y, hi_x, hi_y;
+    float dx, dy;
+};
+
+__device__ __forceinline__ Corners corners(float fx, float fy, int W, int H) {
+    Corners c;
+    const float bx = (float)(W - 1), by = (float)(H - 1);
+    c.hi_x = (int)clampf(ceilf(fx), 0.0f, bx);
+    c.hi_y = (int)clampf(ceilf(fy), 0.0f, by);
+    c.lo_x = (int)clampf(floorf(fx), 0.0f, bx);
+    c.lo_y = (int)clampf(floorf(fy), 0.0f, by);
+    c.dx = fx - (float)c.lo_x;
+    c.dy = fy - (float)c.lo_y;
+    return c;
+}
+
+__device__ __forceinline__ float2 sample_vel(const float2* __restrict__ v, int P,
+                                             const Corners& c) {
+    const float2 lt = __ldg(v + (size_t)c.hi_y * P + c.lo_x);
+    const float2 rt = __ldg(v + (size_t)c.hi_y * P + c.hi_x);
+    const float2 lb = __ldg(v + (size_t)c.lo_y * P + c.lo_x);
+    const float2 rb = __ldg(v + (size_t)c.lo_y * P + c.hi_x);
+    const float h1x = mixf(lt.x, rt.x, c.dx), h1y = mixf(lt.y, rt.y, c.dx);
+    const float h2x = mixf(lb.x, rb.x, c.dx), h2y = mixf(lb.y, rb.y, c.dx);
+    return make_float2(mixf(h2x, h1x, c.dy), mixf(h2y, h1y, c.dy));
+}
+
+__device__ __forceinline__ float sample_scalar(const float* __restrict__ s, int P,
+                                               const Corners& c) {
+    const float lt = __ldg(s + (size_t)c.hi_y * P + c.lo_x);
+    const float rt = __ldg(s + (size_t)c.hi_y * P + c.hi_x);
+    const float lb = __ldg(s + (size_t)c.lo_y * P + c.lo_x);
+    const float rb = __ldg(s + (size_t)c.lo_y * P + c.hi_x);
+    const float h1 = mixf(lt, rt, c.dx);
+    const float h2 = mixf(lb, rb, c.dx);
+    return mixf(h2, h1, c.dy);
+}
+
+// exp for the Gaussian splat weight: Cody-Waite reduction x = k ln2 + r with
+// ln2 = 0.693359375 - 2.12194440e-4 (k*C1 exact), degree-7 Taylor polynomial
+// of exp(r) in Horner form, exact scaling by 2^k.  The oracle evaluates the
+// same sequence, so the weights agree bit for bit.
+__device__ __forceinline__ float nx_expf(float x) {
+    x = x < -87.0f ? -87.0f : x;
+    x = x > 88.0f ? 88.0f : x;
+    const float kf = floorf(x * 1.44269502f + 0.5f);
+    float r = x - kf * 0.693359375f;
+    r = r - kf * -2.12194440e-4f;
+    float p = 0.000198412701f;
+    p = 0.00138888892f + r * p;
+    p = 0.00833333377f + r * p;
+    p = 0.0416666679f + r * p;
+    p = 0.166666672f + r * p;
+    p = 0.5f + r * p;
+    p = 1.0f + r * p;
+    p = 1.0f + r * p;
+    return ldexpf(p, (int)kf);
+}
+
+// Neighbour-substitution flags, one byte per cell, written by the divergence
+// kernel and read by the Jacobi sweeps, the gradient subtraction and the
+// residual.  Bit set <=> that neighbour's pressure is replaced by the centre
+// pressure: the neighbour is an obstacle (shader.Poisson.comp:32-35) or lies
+// beyond a wall, where the clamped index of common.sh:9-19 is the cell itself.
+enum : uint8_t { NB_L = 1, NB_R = 2, NB_B = 4, NB_T = 8 };
+
+}  // namespace natrix

@@ -1,0 +1,237 @@
+// Plain Jacobi pressure sweeps (shader.Poisson.comp:17-38, looped K times by
+// natrix/core/fluid_simulator.py:251-255), temporally blocked.
+//
+// One CTA owns a TX x TY output tile.  A single elected thread issues three
+// TMA tile loads (cp.async.bulk.tensor.2d) of the tile plus a halo of HALO
+// cells: pressure and divergence (float, x-halo rounded up to 4 cells so the
+// box starts on a 16-byte boundary) and the neighbour-substitution flags
+// (uint8, x-halo 16 for the same reason), completing on one mbarrier.  The
+// CTA then runs `sweeps` <= HALO sweeps in shared memory, ping-ponging
+// between two pressure buffers on a region that shrinks by one cell per
+// sweep, and writes the tile interior back with 16-byte stores.  Every sweep
+// evaluates exactly the reference's expression
+//     p' = (pL + pR + pB + pT - b) * 0.25
+// on the same inputs, so k fused sweeps equal k single sweeps bit for bit.
+//
+// TMA fills out-of-grid cells with zeros.  No in-grid cell ever reads them:
+// a cell on a wall has the wall bit in its flags and substitutes its own
+// pressure (the clamped neighbour index of common.sh:9-19 is the cell).
+// Out-of-grid halo cells compute values nobody reads.
+//
+// The mbarrier wait is bounded; on time-out the kernel records status bit 1,
+// waits once more (bounded) for its copies, and returns without writing.
+#include <cudaTypedefs.h>
+
+#include "kernels.cuh"
+
+namespace natrix {
+
+namespace {
+
+constexpr int align128(int b) { return (b + 127) / 128 * 128; }
+
+template <int TX_, int TY_, int HALO_>
+struct JacCfg {
+    static constexpr int TX = TX_, TY = TY_, HALO = HALO_;
+    static constexpr int HXP = (HALO + 3) / 4 * 4;  // x-halo of the float boxes
+    static constexpr int HXF = 16;                    // x-halo of the uint8 box
+    static constexpr int RX = TX + 2 * HXP, RY = TY + 2 * HALO, RXF = TX + 2 * HXF;
+    static constexpr int P_BYTES = RX * RY * 4, F_BYTES = RXF * RY;
+    static constexpr int OFF_A = 0;
+    static constexpr int OFF_B = OFF_A + align128(P_BYTES);
+    static constexpr int OFF_D = OFF_B + align128(P_BYTES);
+    static constexpr int OFF_F = OFF_D + align128(P_BYTES);
+    static constexpr int OFF_BAR = OFF_F + align128(F_BYTES);
+    static constexpr int SMEM = OFF_BAR + 128;
+    static constexpr int THREADS_X = 32, THREADS_Y = 8;
+    static_assert(TX % 16 == 0, "tile width must keep the uint8 box 16-byte aligned");
+    static_assert(RX <= 256 && RY <= 256 && RXF <= 256, "TMA box dimensions are <= 256");
+};
+
+using Cfg = JacCfg<64, 32, 8>;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Bounded wait for phase 0 of the tile barrier (about 4M polls).
+__device__ __forceinline__ bool wait_tile(uint64_t* bar) {
+    for (int it = 0; it < (1 << 22); ++it)
+        if (mbar_try_wait(bar, 0)) return true;
+    return false;
+}
+
+__global__ void __launch_bounds__(Cfg::THREADS_X* Cfg::THREADS_Y)
+    k_jacobi_tb(const __grid_constant__ CUtensorMap tm_p, const __grid_constant__ CUtensorMap tm_div,
+                const __grid_constant__ CUtensorMap tm_flags, float* __restrict__ pout, Grid g,
+                int sweeps, int* __restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    float* A = reinterpret_cast<float*>(smem + Cfg::OFF_A);
+    float* B = reinterpret_cast<float*>(smem + Cfg::OFF_B);
+    const float* D = reinterpret_cast<const float*>(smem + Cfg::OFF_D);
+    const uint8_t* F = reinterpret_cast<const uint8_t*>(smem + Cfg::OFF_F);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Cfg::OFF_BAR);
+    __shared__ int s_ok;
+
+    const int tile_x = blockIdx.x * Cfg::TX, tile_y = blockIdx.y * Cfg::TY;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    if (tx == 0 && ty == 0) {
+        mbar_init(bar, 1);
+        fence_barrier_init();
+        mbar_expect_tx(bar, 2 * Cfg::P_BYTES + Cfg::F_BYTES);
+        tma_load_2d(A, &tm_p, tile_x - Cfg::HXP, tile_y - Cfg::HALO, bar);
+        tma_load_2d(smem + Cfg::OFF_D, &tm_div, tile_x - Cfg::HXP, tile_y - Cfg::HALO, bar);
+        tma_load_2d(smem + Cfg::OFF_F, &tm_flags, tile_x - Cfg::HXF, tile_y - Cfg::HALO, bar);
+        bool ok = wait_tile(bar);
+        if (!ok) {
+            atomicOr(status, 1);
+            wait_tile(bar);  // let the copies land before the CTA exits
+        }
+        s_ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_ok) return;
+
+    constexpr int RX = Cfg::RX, RXF = Cfg::RXF, FOFF = Cfg::HXF - Cfg::HXP;
+    for (int s = 1; s <= sweeps; ++s) {
+        const float* src = (s & 1) ? A : B;
+        float* dst = (s & 1) ? B : A;
+        const int m = sweeps - s;
+        const int x0 = Cfg::HXP - m, x1 = Cfg::HXP + Cfg::TX + m;
+        const int y0 = Cfg::HALO - m, y1 = Cfg::HALO + Cfg::TY + m;
+        for (int yy = y0 + ty; yy < y1; yy += Cfg::THREADS_Y) {
+            for (int xx = x0 + tx; xx < x1; xx += Cfg::THREADS_X) {
+                const int i = yy * RX + xx;
+                const float pc = src[i];
+                const uint8_t f = F[yy * RXF + xx + FOFF];
+                const float l = (f & NB_L) ? pc : src[i - 1];
+                const float r = (f & NB_R) ? pc : src[i + 1];
+                const float b = (f & NB_B) ? pc : src[i - RX];
+                const float t = (f & NB_T) ? pc : src[i + RX];
+                dst[i] = (l + r + b + t - D[i]) * 0.25f;
+            }
+        }
+        __syncthreads();
+    }
+    const float* res = (sweeps & 1) ? B : A;
+
+    // tile interior -> global, 16-byte stores; a float4 group starting inside
+    // the row stays inside the padded pitch (pitch and tile_x are multiples of 4)
+    constexpr int GROUPS = Cfg::TX / 4;
+    for (int k = ty * Cfg::THREADS_X + tx; k < Cfg::TY * GROUPS;
+         k += Cfg::THREADS_X * Cfg::THREADS_Y) {
+        const int row = k / GROUPS, grp = k % GROUPS;
+        const int gy = tile_y + row, gx = tile_x + grp * 4;
+        if (gy >= g.H || gx >= g.W) continue;
+        const float4 v =
+            *reinterpret_cast<const float4*>(res + (Cfg::HALO + row) * RX + Cfg::HXP + grp * 4);
+        *reinterpret_cast<float4*>(pout + (size_t)gy * g.P + gx) = v;
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+bool encode_2d(CUtensorMap* map, CUtensorMapDataType dt, int elem_bytes, void* base, Grid g,
+               int box_x, int box_y, const char** err) {
+    auto fn = get_encode();
+    if (!fn) {
+        *err = "cuTensorMapEncodeTiled is unavailable from the driver";
+        return false;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)g.W, (cuuint64_t)g.H};
+    cuuint64_t strides[1] = {(cuuint64_t)g.P * (cuuint64_t)elem_bytes};
+    cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, dt, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        *err = "cuTensorMapEncodeTiled failed";
+        return false;
+    }
+    return true;
+}
+
+}  // namespace
+
+int jacobi_max_sweeps_per_launch() { return Cfg::HALO; }
+
+bool jacobi_encode_maps(JacobiMaps* maps, float* p0, float* p1, float* div, uint8_t* flags,
+                        Grid g, const char** err) {
+    return encode_2d(&maps->p[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p0, g, Cfg::RX, Cfg::RY,
+                     err) &&
+           encode_2d(&maps->p[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p1, g, Cfg::RX, Cfg::RY,
+                     err) &&
+           encode_2d(&maps->div, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, div, g, Cfg::RX, Cfg::RY,
+                     err) &&
+           encode_2d(&maps->flags, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, flags, g, Cfg::RXF,
+                     Cfg::RY, err);
+}
+
+cudaError_t launch_jacobi(const JacobiMaps& maps, float* const pbuf[2], int src, Grid g,
+                          int sweeps, int* status, cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_jacobi_tb,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    if (sweeps < 1 || sweeps > Cfg::HALO) return cudaErrorInvalidValue;
+    dim3 grid((g.W + Cfg::TX - 1) / Cfg::TX, (g.H + Cfg::TY - 1) / Cfg::TY);
+    dim3 block(Cfg::THREADS_X, Cfg::THREADS_Y);
+    k_jacobi_tb<<<grid, block, Cfg::SMEM, st>>>(maps.p[src], maps.div, maps.flags,
+                                                pbuf[1 - src], g, sweeps, status);
+    return cudaGetLastError();
+}
+
+}  // namespace natrix

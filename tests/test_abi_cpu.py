@@ -1,0 +1,100 @@
+"""Host-side checks that need no GPU: the library loads and exports every
+entry point include/natrix.h declares, the Python surface matches the
+reference's, and parameter validation raises like the reference."""
+from __future__ import annotations
+
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        names |= set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(natrix_\w+)\s*\(", text, re.M))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for must in ("natrix_create", "natrix_step", "natrix_destroy", "natrix_density_step",
+                 "natrix_last_error"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    from natrix_gb300 import _lib
+    from natrix_gb300 import build as nb
+
+    nb.build()
+    lib = _lib.load()
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, f"not exported: {missing}"
+    # every declared symbol has a ctypes signature in the binding
+    unbound = [n for n in declared_symbols() if n not in _lib.SIGNATURES]
+    assert not unbound, f"no ctypes signature: {unbound}"
+    assert lib.natrix_version().startswith(b"natrix_gb300")
+
+
+def test_last_error_is_empty_string_initially():
+    from natrix_gb300 import _lib
+
+    assert isinstance(_lib.load().natrix_last_error(), bytes)
+
+
+def test_create_rejects_bad_sizes_without_gpu():
+    import ctypes
+
+    from natrix_gb300 import _lib
+
+    h = ctypes.c_void_p()
+    rc = _lib.load().natrix_create(0, 5, ctypes.byref(h))
+    assert rc == _lib.NATRIX_EINVAL and not h
+    rc = _lib.load().natrix_create(40000, 5, ctypes.byref(h))
+    assert rc == _lib.NATRIX_ERANGE
+
+
+def _bare(cls):
+    return object.__new__(cls)
+
+
+@pytest.mark.parametrize("prop,bad,msg", [
+    ("speed", 0, "'Speed' should be greater than zero"),
+    ("iterations", 0, "'Iterations' should be grater than zero"),
+    ("dissipation", -1.0, "'Dissipation' should be grater than zero"),
+    ("vorticity", -0.1, "'Vorticity' should be grater or equal than zero"),
+    ("viscosity", -0.1, "'Viscosity' should be greater or equal than zero"),
+])
+def test_property_validation_matches_reference(prop, bad, msg):
+    from natrix_gb300 import FluidSimulator
+
+    sim = _bare(FluidSimulator)
+    with pytest.raises(ValueError, match=re.escape(msg)):
+        setattr(sim, prop, bad)
+    setattr(sim, prop, {"speed": 3.0, "iterations": 7, "dissipation": 0.5,
+                        "vorticity": 0.0, "viscosity": 0.0}[prop])
+
+
+def test_defaults_match_reference():
+    from natrix_gb300 import FluidSimulator, SmoothParticlesArea
+
+    sim = _bare(FluidSimulator)
+    assert (sim.speed, sim.iterations, sim.dissipation, sim.vorticity, sim.viscosity) == (
+        500.0, 50, 1.0, 0.0, 0.1)
+    assert FluidSimulator.has_borders is True and FluidSimulator.simulate is True
+    d = _bare(SmoothParticlesArea)
+    assert (d.speed, d.dissipation) == (500.0, 1.0)
+    with pytest.raises(ValueError, match="'Dissipation' should be grater than zero"):
+        d.dissipation = 0
+
+
+def test_reference_import_path():
+    from natrix.core.fluid_simulator import FluidSimulator as A
+
+    from natrix_gb300 import FluidSimulator as B
+
+    assert A is B

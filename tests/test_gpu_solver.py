@@ -1,0 +1,319 @@
+"""GPU parity of the solver through the public API / C ABI.
+
+Bit-exact (==, so +0 and -0 compare equal) against the float32 oracle and
+against the golden vectors written from the reference's own shaders; within
+the stated tolerance against the float64 oracle."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests.golden_replay import assert_equal_f32, replay_steps
+
+pytestmark = pytest.mark.gpu
+
+
+def make_pair(oracle, W, H, dtype=np.float32, **params):
+    from natrix_gb300 import FluidSimulator, SmoothParticlesArea
+
+    sim = FluidSimulator(W, H)
+    den = SmoothParticlesArea(W, H, sim)
+    ref = oracle.OracleFluid(W, H, dtype)
+    rden = oracle.OracleDensity(W, H, ref)
+    for s in (sim, ref):
+        for k, v in params.items():
+            setattr(s, k, v)
+    for d in (den, rden):
+        d.speed = params.get("speed", 500.0)
+        d.dissipation = params.get("dissipation", 1.0)
+    return sim, den, ref, rden
+
+
+def run_workload(sim, den, ref, rden, steps, n_splats, n_obst, seed, sweeps_per_launch=0):
+    from natrix_gb300 import workloads as wl
+
+    W, H = sim.width, sim.height
+    sim.sweeps_per_launch = sweeps_per_launch
+    rng = np.random.default_rng(seed)
+    obst = wl.circle_obstacles(rng, n_obst, W, H, 0.05, 0.12) if n_obst else np.zeros((0, 3))
+    for _ in range(steps):
+        splats = wl.gauss_splats(rng, n_splats, W, H, 5.0)
+        for s in (sim, ref):
+            for o in obst:
+                s.add_circle_obstacle((float(o[0]), float(o[1])), float(o[2]))
+        sim.add_splats(splats, den)
+        ref.add_splats(splats, rden)
+        sim.update(1 / 60)
+        den.update(1 / 60)
+        ref.update(1 / 60)
+        rden.update(1 / 60)
+
+
+def fields(sim, den):
+    from natrix_gb300 import _lib
+
+    out = {
+        "velocity": sim.download(_lib.FIELD_VELOCITY),
+        "pressure": sim.download(_lib.FIELD_PRESSURE),
+        "divergence": sim.download(_lib.FIELD_DIVERGENCE),
+        "density": den.download(),
+    }
+    if sim.vorticity > 0:
+        out["vorticity"] = sim.download(_lib.FIELD_VORTICITY)
+    sim.sync()
+    return out
+
+
+def ref_fields(ref, rden):
+    return {"velocity": ref.velocity, "pressure": ref.pressure, "divergence": ref.divergence,
+            "density": rden.field, "vorticity": ref.vorticity_field}
+
+
+@pytest.mark.parametrize("name", ["steps_48x40.npz", "steps_33x29_defaults.npz"])
+def test_golden_steps_on_gpu(cuda, golden_dir, name):
+    """The reference shaders' own outputs (golden vectors), replayed through
+    the drop-in API: obstacles, add_velocity, add_particles, update."""
+    from natrix_gb300 import FluidSimulator, SmoothParticlesArea
+
+    d = np.load(golden_dir / name)
+    H, W = d["vel_1"].shape[:2]
+    sim = FluidSimulator(W, H)
+    den = SmoothParticlesArea(W, H, sim)
+
+    def check(step):
+        got = fields(sim, den)
+        assert_equal_f32(got["velocity"], d[f"vel_{step}"], f"velocity step {step}")
+        assert_equal_f32(got["pressure"], d[f"pressure_{step}"], f"pressure step {step}")
+        assert_equal_f32(got["divergence"], d[f"div_{step}"], f"divergence step {step}")
+        assert_equal_f32(got["density"], d[f"density_{step}"], f"density step {step}")
+        if sim.vorticity > 0:
+            assert_equal_f32(got["vorticity"], d[f"vort_{step}"], f"vorticity step {step}")
+
+    assert replay_steps(d, sim, den, check)
+    den.destroy()
+    sim.destroy()
+
+
+CASES = [
+    # W, H, iterations, vorticity, viscosity, obstacles, sweeps_per_launch
+    (64, 64, 40, 0.0, 0.0, 0, 0),
+    (97, 61, 17, 0.35, 0.0, 3, 0),
+    (130, 75, 9, 0.35, 0.1, 4, 3),
+    (33, 190, 8, 0.0, 0.1, 2, 1),
+    (256, 256, 40, 0.0, 0.0, 0, 0),
+    (200, 144, 80, 0.35, 0.0, 6, 8),
+]
+
+
+@pytest.mark.parametrize("W,H,K,eps,nu,nobs,spl", CASES)
+def test_steps_bit_exact_vs_oracle(cuda, oracle, W, H, K, eps, nu, nobs, spl):
+    sim, den, ref, rden = make_pair(oracle, W, H, iterations=K, vorticity=eps, viscosity=nu,
+                                    speed=5.0, dissipation=0.99)
+    run_workload(sim, den, ref, rden, steps=6, n_splats=6, n_obst=nobs, seed=W * 7 + H,
+                 sweeps_per_launch=spl)
+    got, want = fields(sim, den), ref_fields(ref, rden)
+    for k, v in got.items():
+        assert_equal_f32(v, want[k], k)
+    den.destroy()
+    sim.destroy()
+
+
+def test_temporal_blocking_is_bit_identical(cuda, oracle):
+    """k fused sweeps per launch == k single-sweep launches, for every k."""
+    from natrix_gb300 import _lib
+
+    results = []
+    for spl in (1, 2, 5, 8):
+        sim, den, ref, rden = make_pair(oracle, 150, 90, iterations=37, vorticity=0.2,
+                                        viscosity=0.0, speed=5.0, dissipation=0.99)
+        run_workload(sim, den, ref, rden, steps=2, n_splats=5, n_obst=3, seed=5,
+                     sweeps_per_launch=spl)
+        results.append(sim.download(_lib.FIELD_PRESSURE))
+        den.destroy()
+        sim.destroy()
+    for r in results[1:]:
+        assert_equal_f32(r, results[0], "pressure with another sweeps_per_launch")
+
+
+def test_jacobi_sweeps_isolated(cuda, oracle):
+    """natrix_jacobi on an uploaded pressure/divergence equals the oracle's
+    sweeps with the last step's obstacles, for several sweep counts."""
+    from natrix_gb300 import _lib
+
+    W, H = 123, 77
+    sim, den, ref, rden = make_pair(oracle, W, H, iterations=1, speed=5.0)
+    rng = np.random.default_rng(9)
+    for s in (sim, ref):
+        s.add_circle_obstacle((0.3, 0.4), 9.0)
+        s.add_triangle_obstacle((0.6, 0.1), (0.9, 0.2), (0.7, 0.6), True)
+        s.update(1 / 60)
+    mask = np.zeros((H, W), np.uint8)
+    oracle.add_circle_obstacle(mask, 0.3, 0.4, 9.0)
+    oracle.add_triangle_obstacle(mask, (0.6, 0.1), (0.9, 0.2), (0.7, 0.6), True)
+    for sweeps in (1, 7, 8, 9, 30):
+        p = rng.normal(size=(H, W)).astype(np.float32)
+        b = rng.normal(size=(H, W)).astype(np.float32)
+        sim.upload(_lib.FIELD_PRESSURE, p)
+        sim.upload(_lib.FIELD_DIVERGENCE, b)
+        sim.jacobi(sweeps)
+        got = sim.download(_lib.FIELD_PRESSURE)
+        assert_equal_f32(got, oracle.jacobi_n(p, b, mask, sweeps), f"{sweeps} sweeps")
+        # residual sums against the oracle's (double accumulation, order differs)
+        rs = sim.residual_sums()
+        want = oracle.residual_sums(got, b, mask)
+        np.testing.assert_allclose(rs, want, rtol=1e-9, atol=1e-9)
+    sim.sync()
+    den.destroy()
+    sim.destroy()
+
+
+def test_float64_tolerance(cuda, oracle):
+    """GPU float32 vs the float64 oracle after 1 and 10 steps: per-field
+    max-abs <= 1e-4 x field scale and rel-L2 <= 1e-5."""
+    W, H = 128, 128
+    sim, den, ref, rden = make_pair(oracle, W, H, np.float64, iterations=40, vorticity=0.35,
+                                    viscosity=0.0, speed=5.0, dissipation=0.99)
+    from natrix_gb300 import workloads as wl
+
+    rng = np.random.default_rng(4)
+    obst = wl.circle_obstacles(rng, 4, W, H, 0.03, 0.08)
+    for step in range(1, 11):
+        splats = wl.gauss_splats(rng, 8, W, H, 5.0)
+        for s in (sim, ref):
+            for o in obst:
+                s.add_circle_obstacle((float(o[0]), float(o[1])), float(o[2]))
+        sim.add_splats(splats, den)
+        ref.add_splats(splats, rden)
+        for x in (sim, den, ref, rden):
+            x.update(1 / 60)
+        if step in (1, 10):
+            got, want = fields(sim, den), ref_fields(ref, rden)
+            for k, v in got.items():
+                w = want[k]
+                scale = max(float(np.max(np.abs(w))), 1e-30)
+                maxabs = float(np.max(np.abs(v - w)))
+                rel = float(np.linalg.norm((v - w).ravel()) / max(np.linalg.norm(w), 1e-30))
+                assert maxabs <= 1e-4 * scale, f"{k} step {step}: max-abs {maxabs:.3g}"
+                assert rel <= 1e-5, f"{k} step {step}: rel-L2 {rel:.3g}"
+    den.destroy()
+    sim.destroy()
+
+
+def test_decoupled_density_grid(cuda, oracle):
+    """Density on its own grid size (demo/smooth_particles_area.py keeps the
+    framebuffer size while velocity runs at half the window size)."""
+    from natrix_gb300 import FluidSimulator, SmoothParticlesArea
+
+    Wv, Hv, Wp, Hp = 64, 36, 128, 72
+    sim = FluidSimulator(Wv, Hv)
+    den = SmoothParticlesArea(Wp, Hp, sim)
+    ref = oracle.OracleFluid(Wv, Hv, np.float32)
+    rden = oracle.OracleDensity(Wp, Hp, ref)
+    for s in (sim, ref):
+        s.iterations, s.vorticity, s.viscosity = 20, 1.0, 0.5
+    for d in (den, rden):
+        d.dissipation = 0.98
+    for step in range(5):
+        for s in (sim, ref):
+            s.add_circle_obstacle((0.5, 0.5), 6.0)
+            s.update(1 / 60)
+        for d in (den, rden):
+            d.update(1 / 60)
+        for s in (sim, ref):
+            s.add_velocity((0.3, 0.6), (0.2 * step, -0.1), 10.0)
+        for d in (den, rden):
+            d.add_particles((0.3, 0.6), 20.0, 100.0)
+    assert_equal_f32(den.download(), rden.field, "decoupled density")
+    den.destroy()
+    sim.destroy()
+
+
+def test_flags_borders_and_simulate(cuda, oracle):
+    from natrix_gb300 import _lib
+
+    sim, den, ref, rden = make_pair(oracle, 40, 30, iterations=12, speed=50.0)
+    sim.has_borders = ref.has_borders = False
+    for s in (sim, ref):
+        s.add_velocity((0.02, 0.5), (1.0, 0.3), 12.0)
+        s.update(1 / 60)
+    assert_equal_f32(sim.download(_lib.FIELD_VELOCITY), ref.velocity, "has_borders=False")
+    before = sim.download(_lib.FIELD_VELOCITY)
+    sim.simulate = False
+    sim.add_velocity((0.5, 0.5), (1.0, 1.0), 10.0)
+    sim.update(1 / 60)
+    assert_equal_f32(sim.download(_lib.FIELD_VELOCITY), before, "simulate=False is a no-op")
+    den.destroy()
+    sim.destroy()
+
+
+@pytest.mark.parametrize("W,H", [(1, 1), (2, 3), (5, 1), (1, 7), (17, 23)])
+def test_tiny_and_odd_grids(cuda, oracle, W, H):
+    sim, den, ref, rden = make_pair(oracle, W, H, iterations=10, vorticity=0.3,
+                                    viscosity=0.1, speed=5.0)
+    for step in range(3):
+        for s in (sim, ref):
+            s.add_velocity((0.5, 0.5), (0.7, -0.4), 3.0)
+            s.add_circle_obstacle((0.1, 0.1), 0.5)
+            s.update(1 / 60)
+        for d in (den, rden):
+            d.add_particles((0.5, 0.5), 2.0, 10.0)
+            d.update(1 / 60)
+    got, want = fields(sim, den), ref_fields(ref, rden)
+    for k, v in got.items():
+        assert_equal_f32(v, want[k], f"{k} {W}x{H}")
+    den.destroy()
+    sim.destroy()
+
+
+def test_field_views_alias_device_state(cuda):
+    from natrix_gb300 import FluidSimulator
+
+    sim = FluidSimulator(48, 32)
+    sim.add_velocity((0.5, 0.5), (0.5, 0.25), 8.0)
+    v = sim.get_velocity_buffer()
+    assert v.shape == (32, 48, 2) and v.is_cuda
+    assert float(v.abs().max()) > 0
+    sim.destroy()
+
+
+@pytest.mark.slow
+def test_full_size_2048_bit_exact_and_tolerance(cuda, oracle):
+    """The 2048x2048 workload (eps 0.35, 80 sweeps, 12 discs, 16 splats per
+    step): bit-exact with the float32 oracle and within tolerance of the
+    float64 oracle after steps 1 and 10."""
+    from natrix_gb300 import FluidSimulator, SmoothParticlesArea
+    from natrix_gb300 import workloads as wl
+
+    spec = wl.LARGE_2048
+    W, H = spec.width, spec.height
+    sim = FluidSimulator(W, H)
+    den = SmoothParticlesArea(W, H, sim)
+    r32 = oracle.OracleFluid(W, H, np.float32)
+    d32 = oracle.OracleDensity(W, H, r32)
+    r64 = oracle.OracleFluid(W, H, np.float64)
+    d64 = oracle.OracleDensity(W, H, r64)
+    for s in (sim, r32, r64):
+        s.iterations, s.vorticity, s.viscosity = spec.iterations, spec.vorticity, spec.viscosity
+        s.speed, s.dissipation = spec.speed, spec.dissipation
+    for d in (den, d32, d64):
+        d.speed, d.dissipation = spec.speed, spec.dissipation
+    obst = wl.workload_obstacles(0, spec)
+    for step in range(1, 11):
+        splats = wl.step_forcing(0, step - 1, spec)
+        for s in (sim, r32, r64):
+            for o in obst:
+                s.add_circle_obstacle((float(o[0]), float(o[1])), float(o[2]))
+        sim.add_splats(splats, den)
+        r32.add_splats(splats, d32)
+        r64.add_splats(splats, d64)
+        for x in (sim, den, r32, d32, r64, d64):
+            x.update(spec.dt)
+        if step in (1, 10):
+            got = fields(sim, den)
+            for k, v in got.items():
+                assert_equal_f32(v, ref_fields(r32, d32)[k], f"{k} step {step} vs float32")
+                w = ref_fields(r64, d64)[k]
+                scale = max(float(np.max(np.abs(w))), 1e-30)
+                assert float(np.max(np.abs(v - w))) <= 1e-4 * scale, f"{k} step {step} vs f64"
+    den.destroy()
+    sim.destroy()
