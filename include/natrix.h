@@ -176,6 +176,31 @@ int natrix_set_timing(natrix_sim* sim, int32_t enable);
 /* Read the counters (waits for the timed events); reset = 1 zeroes them. */
 int natrix_get_stats(natrix_sim* sim, natrix_stats* out, int32_t reset);
 
+/* Largest grid, in cells, that natrix_residual_noalloc accepts (4096 x 4096). */
+#define NATRIX_NOALLOC_MAX_CELLS (4096 * 4096)
+
+/* Residual sums of a pressure system, computed without allocating anything.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc (code running inside another framework's memory pool, plugins
+ * that must not touch the allocator, hosts with a fixed device budget) and so
+ * cannot create a simulator handle, whose natrix_residual uses scratch that
+ * natrix_create allocated.  Here the caller passes its own device buffers:
+ * pressure `p` and divergence `div` (float, rows of `pitch` elements), an
+ * optional obstacle mask (uint8, same pitch in bytes; NULL = no obstacles)
+ * and `out_dev`, 5 doubles in device memory that receive
+ * {n, sum r, sum r^2, sum b, sum b^2} exactly as natrix_residual defines them.
+ * The scratch is a fixed array inside the library, sized for grids of up to
+ * NATRIX_NOALLOC_MAX_CELLS cells (larger grids return NATRIX_ERANGE); it
+ * stays resident on every GPU that loads the library until the process exits.
+ * All calls share that array, so calls whose kernels overlap on the GPU race
+ * and may return wrong sums: order them on one stream.  The first call on a
+ * device looks up the array's device address (with that device current);
+ * make that first call before any stream capture.  Stream-ordered on
+ * `stream`; runs on the calling thread's current device. */
+int natrix_residual_noalloc(const float* p, const float* div, const uint8_t* mask,
+                            int32_t width, int32_t height, int64_t pitch, double* out_dev,
+                            void* stream);
+
 /* Message of the calling thread's last error ("" if none). */
 const char* natrix_last_error(void);
 

@@ -82,6 +82,7 @@ SIGNATURES = {
     "natrix_density_field": [_vp, _vpp, _i64p],
     "natrix_density_upload": [_vp, _vp, _vp],
     "natrix_density_download": [_vp, _vp, _vp],
+    "natrix_residual_noalloc": [_vp, _vp, _vp, _i, _i, ctypes.c_int64, _vp, _vp],
     "natrix_last_error": [],
     "natrix_version": [],
 }

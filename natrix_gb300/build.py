@@ -27,6 +27,7 @@ UNITS = {
     "solver_kernels.cu": ["-fmad=false"],
     "jacobi_tma.cu": ["-fmad=false"],
     "capi.cu": [],
+    "noalloc.cu": ["-fmad=false"],
 }
 
 

@@ -42,6 +42,15 @@ int fail(int code, const char* fmt, ...) {
     return code;
 }
 
+}  // namespace
+
+int natrix::set_last_error(int code, const char* msg) {
+    g_err = msg;
+    return code;
+}
+
+namespace {
+
 int cuda_fail(cudaError_t e, const char* what) {
     return fail(NATRIX_ECUDA, "%s: %s", what, cudaGetErrorString(e));
 }

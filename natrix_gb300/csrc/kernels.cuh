@@ -52,6 +52,9 @@ struct ShapeOp {
 // applies the ops in order).
 constexpr int kMaxOpsPerLaunch = 256;
 
+// Record `msg` as the calling thread's natrix_last_error() and return `code`.
+int set_last_error(int code, const char* msg);
+
 // ---- per-cell kernels (solver_kernels.cu) --------------------------------
 cudaError_t launch_obstacles(uint8_t* mask, Grid g, const ShapeOp* ops, int n, int fresh,
                              cudaStream_t st);
