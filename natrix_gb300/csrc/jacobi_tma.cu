@@ -22,6 +22,8 @@
 // waits once more (bounded) for its copies, and returns without writing.
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
+
 #include "kernels.cuh"
 
 namespace natrix {
@@ -166,6 +168,155 @@ __global__ void __launch_bounds__(Cfg::THREADS_X* Cfg::THREADS_Y)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Register-tiled variant.  The CTA region is 128 columns x NW*R rows; warp w
+// owns rows [w*R, w*R + R), lane l owns columns [4l, 4l + 4), so every cell
+// of the region lives in one thread's registers for all the launch's sweeps.
+// Per sweep a thread needs, per row, its left/right neighbours (warp shuffles
+// of the adjacent lanes' edge columns), the rows above/below (its own
+// registers, or the neighbouring warps' edge rows exchanged through a
+// double-buffered shared-memory slot: one barrier per sweep) and the
+// divergence (shared memory).  Rows whose warp holds no wall / obstacle
+// neighbour take a substitution-free path (warp-uniform branch).  Cells near
+// the region edge compute values from missing neighbours; after s sweeps the
+// outer s rows/columns are invalid and the output tile (HALO rows / HXP
+// columns in) stays exact for s <= HALO.
+template <int R_, int NW_, int HALO_>
+struct RtCfg {
+    static constexpr int R = R_, NW = NW_, HALO = HALO_;
+    static constexpr int RX = 128, RY = NW * R;
+    static constexpr int HXP = (HALO + 3) / 4 * 4;
+    static constexpr int TX = RX - 2 * HXP, TY = RY - 2 * HALO;
+    static constexpr int HXF = 16, RXF = TX + 2 * HXF;
+    static constexpr int P_BYTES = RX * RY * 4, F_BYTES = RXF * RY;
+    static constexpr int X_FLOATS = 2 * NW * 2 * RX;  // [slot][warp][top,bottom][RX]
+    static constexpr int OFF_P = 0;
+    static constexpr int OFF_D = OFF_P + align128(P_BYTES);
+    static constexpr int OFF_F = OFF_D + align128(P_BYTES);
+    static constexpr int OFF_X = OFF_F + align128(F_BYTES);
+    static constexpr int OFF_BAR = OFF_X + align128(X_FLOATS * 4);
+    static constexpr int SMEM = OFF_BAR + 128;
+    static constexpr int THREADS = NW * 32;
+    static_assert(TX % 16 == 0, "tile width must keep the uint8 box 16-byte aligned");
+    static_assert(RY <= 256 && RXF <= 256, "TMA box dimensions are <= 256");
+    static_assert(TY > 0, "region too short for the halo");
+};
+
+using RtBig = RtCfg<8, 16, 8>;
+
+template <class C>
+__global__ void __launch_bounds__(C::THREADS, 1)
+    k_jacobi_rt(const __grid_constant__ CUtensorMap tm_p, const __grid_constant__ CUtensorMap tm_div,
+                const __grid_constant__ CUtensorMap tm_flags, float* __restrict__ pout, Grid g,
+                int sweeps, int* __restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const float* Ps = reinterpret_cast<const float*>(smem + C::OFF_P);
+    const float* Ds = reinterpret_cast<const float*>(smem + C::OFF_D);
+    const uint8_t* Fs = reinterpret_cast<const uint8_t*>(smem + C::OFF_F);
+    float* X = reinterpret_cast<float*>(smem + C::OFF_X);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+    __shared__ int s_ok;
+
+    const int tile_x = blockIdx.x * C::TX, tile_y = blockIdx.y * C::TY;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_barrier_init();
+        mbar_expect_tx(bar, 2 * C::P_BYTES + C::F_BYTES);
+        tma_load_2d(smem + C::OFF_P, &tm_p, tile_x - C::HXP, tile_y - C::HALO, bar);
+        tma_load_2d(smem + C::OFF_D, &tm_div, tile_x - C::HXP, tile_y - C::HALO, bar);
+        tma_load_2d(smem + C::OFF_F, &tm_flags, tile_x - C::HXF, tile_y - C::HALO, bar);
+        bool ok = wait_tile(bar);
+        if (!ok) {
+            atomicOr(status, 1);
+            wait_tile(bar);
+        }
+        s_ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_ok) return;
+
+    constexpr int R = C::R, RX = C::RX;
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int c0 = lane * 4, r0 = w * R;
+    float p[R][4];
+    uint32_t f[R];
+    uint32_t slow = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const float4 v = *reinterpret_cast<const float4*>(Ps + (r0 + r) * RX + c0);
+        p[r][0] = v.x;
+        p[r][1] = v.y;
+        p[r][2] = v.z;
+        p[r][3] = v.w;
+        f[r] = *reinterpret_cast<const uint32_t*>(Fs + (r0 + r) * C::RXF + c0 + (C::HXF - C::HXP));
+        if (__any_sync(FULL, f[r] != 0u)) slow |= 1u << r;
+    }
+
+    for (int s = 0; s < sweeps; ++s) {
+        float* xs = X + (s & 1) * (C::NW * 2 * RX);
+        *reinterpret_cast<float4*>(xs + (w * 2 + 0) * RX + c0) =
+            make_float4(p[0][0], p[0][1], p[0][2], p[0][3]);
+        *reinterpret_cast<float4*>(xs + (w * 2 + 1) * RX + c0) =
+            make_float4(p[R - 1][0], p[R - 1][1], p[R - 1][2], p[R - 1][3]);
+        __syncthreads();
+        float up[4], below[4];
+        {
+            const float4 a = w > 0 ? *reinterpret_cast<const float4*>(xs + ((w - 1) * 2 + 1) * RX + c0)
+                                   : make_float4(p[0][0], p[0][1], p[0][2], p[0][3]);
+            const float4 b = w < C::NW - 1
+                                 ? *reinterpret_cast<const float4*>(xs + ((w + 1) * 2 + 0) * RX + c0)
+                                 : make_float4(p[R - 1][0], p[R - 1][1], p[R - 1][2], p[R - 1][3]);
+            up[0] = a.x; up[1] = a.y; up[2] = a.z; up[3] = a.w;
+            below[0] = b.x; below[1] = b.y; below[2] = b.z; below[3] = b.w;
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            float cur[4], dn[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                cur[j] = p[r][j];
+                dn[j] = r < R - 1 ? p[r + 1][j] : below[j];
+            }
+            const float lft = __shfl_up_sync(FULL, cur[3], 1);
+            const float rgt = __shfl_down_sync(FULL, cur[0], 1);
+            const float4 dv = *reinterpret_cast<const float4*>(Ds + (r0 + r) * RX + c0);
+            const float d[4] = {dv.x, dv.y, dv.z, dv.w};
+            const float L[4] = {lft, cur[0], cur[1], cur[2]};
+            const float Rn[4] = {cur[1], cur[2], cur[3], rgt};
+            if (slow & (1u << r)) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const uint32_t fb = f[r] >> (8 * j);
+                    const float l = (fb & NB_L) ? cur[j] : L[j];
+                    const float rr = (fb & NB_R) ? cur[j] : Rn[j];
+                    const float b = (fb & NB_B) ? cur[j] : up[j];
+                    const float t = (fb & NB_T) ? cur[j] : dn[j];
+                    p[r][j] = (l + rr + b + t - d[j]) * 0.25f;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) p[r][j] = (L[j] + Rn[j] + up[j] + dn[j] - d[j]) * 0.25f;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) up[j] = cur[j];
+        }
+    }
+
+    // output tile: region rows [HALO, HALO + TY), columns [HXP, HXP + TX)
+    if (c0 >= C::HXP && c0 < C::HXP + C::TX) {
+        const int gx = tile_x + c0 - C::HXP;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int rr = r0 + r;
+            const int gy = tile_y + rr - C::HALO;
+            if (rr >= C::HALO && rr < C::HALO + C::TY && gy < g.H && gx < g.W)
+                *reinterpret_cast<float4*>(pout + (size_t)gy * g.P + gx) =
+                    make_float4(p[r][0], p[r][1], p[r][2], p[r][3]);
+        }
+    }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
@@ -200,20 +351,30 @@ bool encode_2d(CUtensorMap* map, CUtensorMapDataType dt, int elem_bytes, void* b
     return true;
 }
 
+// Kernel variant: 0 = shared-memory sweeps (k_jacobi_tb), 1 = register tiled
+// (k_jacobi_rt, default).  NATRIX_JACOBI_VARIANT selects one for comparison.
+int variant() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("NATRIX_JACOBI_VARIANT");
+        v = (e && e[0] == '0') ? 0 : 1;
+    }
+    return v;
+}
+
 }  // namespace
 
-int jacobi_max_sweeps_per_launch() { return Cfg::HALO; }
+int jacobi_max_sweeps_per_launch() { return Cfg::HALO < RtBig::HALO ? Cfg::HALO : RtBig::HALO; }
 
 bool jacobi_encode_maps(JacobiMaps* maps, float* p0, float* p1, float* div, uint8_t* flags,
                         Grid g, const char** err) {
-    return encode_2d(&maps->p[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p0, g, Cfg::RX, Cfg::RY,
-                     err) &&
-           encode_2d(&maps->p[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p1, g, Cfg::RX, Cfg::RY,
-                     err) &&
-           encode_2d(&maps->div, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, div, g, Cfg::RX, Cfg::RY,
-                     err) &&
-           encode_2d(&maps->flags, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, flags, g, Cfg::RXF,
-                     Cfg::RY, err);
+    const bool rt = variant() == 1;
+    const int bx = rt ? RtBig::RX : Cfg::RX, by = rt ? RtBig::RY : Cfg::RY;
+    const int bfx = rt ? RtBig::RXF : Cfg::RXF;
+    return encode_2d(&maps->p[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p0, g, bx, by, err) &&
+           encode_2d(&maps->p[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p1, g, bx, by, err) &&
+           encode_2d(&maps->div, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, div, g, bx, by, err) &&
+           encode_2d(&maps->flags, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, flags, g, bfx, by, err);
 }
 
 cudaError_t launch_jacobi(const JacobiMaps& maps, float* const pbuf[2], int src, Grid g,
@@ -223,14 +384,23 @@ cudaError_t launch_jacobi(const JacobiMaps& maps, float* const pbuf[2], int src,
         cudaError_t e = cudaFuncSetAttribute(k_jacobi_tb,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              Cfg::SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_jacobi_rt<RtBig>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, RtBig::SMEM);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    if (sweeps < 1 || sweeps > Cfg::HALO) return cudaErrorInvalidValue;
-    dim3 grid((g.W + Cfg::TX - 1) / Cfg::TX, (g.H + Cfg::TY - 1) / Cfg::TY);
-    dim3 block(Cfg::THREADS_X, Cfg::THREADS_Y);
-    k_jacobi_tb<<<grid, block, Cfg::SMEM, st>>>(maps.p[src], maps.div, maps.flags,
-                                                pbuf[1 - src], g, sweeps, status);
+    if (sweeps < 1 || sweeps > jacobi_max_sweeps_per_launch()) return cudaErrorInvalidValue;
+    if (variant() == 1) {
+        dim3 grid((g.W + RtBig::TX - 1) / RtBig::TX, (g.H + RtBig::TY - 1) / RtBig::TY);
+        k_jacobi_rt<RtBig><<<grid, RtBig::THREADS, RtBig::SMEM, st>>>(
+            maps.p[src], maps.div, maps.flags, pbuf[1 - src], g, sweeps, status);
+    } else {
+        dim3 grid((g.W + Cfg::TX - 1) / Cfg::TX, (g.H + Cfg::TY - 1) / Cfg::TY);
+        dim3 block(Cfg::THREADS_X, Cfg::THREADS_Y);
+        k_jacobi_tb<<<grid, block, Cfg::SMEM, st>>>(maps.p[src], maps.div, maps.flags,
+                                                    pbuf[1 - src], g, sweeps, status);
+    }
     return cudaGetLastError();
 }
 

@@ -24,19 +24,62 @@ __device__ __forceinline__ float tri_sign(float p1x, float p1y, float p2x, float
     return ((p1x - p3x) * (p2y - p3y)) - ((p2x - p3x) * (p1y - p3y));
 }
 
+// Block-level culling: warp 0 compacts, in order, the indices of the ops
+// whose conservative footprint (expanded by one cell) meets this block's
+// cells; `test(k)` decides.  Every cell then walks the kept list only.
+template <class Test>
+__device__ __forceinline__ int cull_ops(int n, int* kept, Test test) {
+    __shared__ int s_n;
+    if (threadIdx.y == 0) {
+        int count = 0;
+        for (int base = 0; base < n; base += 32) {
+            const int k = base + threadIdx.x;
+            const bool keep = k < n && test(k);
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep) kept[count + __popc(m & ((1u << threadIdx.x) - 1u))] = k;
+            count += __popc(m);
+        }
+        if (threadIdx.x == 0) s_n = count;
+    }
+    __syncthreads();
+    return s_n;
+}
+
+// Does a disc of radius `r` around (cx, cy) meet the cell box [x0,x1]x[y0,y1]?
+// (conservative: one cell of margin)
+__device__ __forceinline__ bool disc_meets_box(float cx, float cy, float r, int x0, int x1,
+                                               int y0, int y1) {
+    const float dx = fmaxf(fmaxf((float)x0 - cx, cx - (float)x1), 0.0f);
+    const float dy = fmaxf(fmaxf((float)y0 - cy, cy - (float)y1), 0.0f);
+    const float rr = r + 1.0f;
+    return dx * dx + dy * dy <= rr * rr;
+}
+
 __global__ void __launch_bounds__(BX* BY)
     k_obstacles(uint8_t* __restrict__ mask, Grid g, const ShapeOp* __restrict__ ops, int n,
                 int fresh) {
     __shared__ ShapeOp s_ops[kMaxOpsPerLaunch];
+    __shared__ int s_kept[kMaxOpsPerLaunch];
     const int tid = threadIdx.y * BX + threadIdx.x;
     for (int i = tid; i < n; i += BX * BY) s_ops[i] = ops[i];
     __syncthreads();
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+    const int bx0 = blockIdx.x * BX, by0 = blockIdx.y * BY;
+    const int bx1 = bx0 + BX - 1, by1 = by0 + BY - 1;
+    const int nk = cull_ops(n, s_kept, [&](int k) {
+        const ShapeOp& op = s_ops[k];
+        // triangles are never culled: the reference's same-sign test marks
+        // cells far outside a degenerate (zero-area) triangle's bounding box
+        if (op.kind != SHAPE_CIRCLE) return true;
+        return disc_meets_box(op.a[0] * (float)g.W, op.a[1] * (float)g.H, op.a[2], bx0, bx1,
+                              by0, by1);
+    });
+    const int x = bx0 + threadIdx.x, y = by0 + threadIdx.y;
     if (x >= g.W || y >= g.H) return;
     const size_t i = (size_t)y * g.P + x;
+    if (nk == 0 && !fresh) return;
     uint8_t m = fresh ? 0 : mask[i];
-    for (int k = 0; k < n; ++k) {
-        const ShapeOp& op = s_ops[k];
+    for (int kk = 0; kk < nk; ++kk) {
+        const ShapeOp& op = s_ops[s_kept[kk]];
         if (op.kind == SHAPE_CIRCLE) {
             const float spx = op.a[0] * (float)g.W, spy = op.a[1] * (float)g.H;
             const float dx = spx - (float)x, dy = spy - (float)y;
@@ -61,67 +104,119 @@ __global__ void __launch_bounds__(BX* BY)
 //      for every cell, rho = clamp(rho + w s, 0, 255) inside the cut-off.
 //  FORCE_CONE_DENSITY   demo/shaders/shader.AddParticle.comp:25-34 on rows the
 //      reference's dispatch reaches.
+// Ops whose footprint misses the block are culled.  For velocity that is
+// exact because a velocity op outside its footprint is a clamp, and clamp is
+// idempotent: the only trace a culled or missing op leaves is the clamp of the
+// first velocity op when it does not touch the cell (a cell whose first op
+// touches it starts from the unclamped value, as in the reference).
+__device__ __forceinline__ bool op_is_velocity(int kind) {
+    return kind == FORCE_CONE_VELOCITY || kind == FORCE_GAUSS;
+}
+
 __global__ void __launch_bounds__(BX* BY)
     k_forcing(float2* __restrict__ vel, Grid gv, float* __restrict__ rho, Grid gd,
               const ForceOp* __restrict__ ops, int n) {
     __shared__ ForceOp s_ops[kMaxOpsPerLaunch];
+    __shared__ int s_kept[kMaxOpsPerLaunch];
     const int tid = threadIdx.y * BX + threadIdx.x;
     for (int i = tid; i < n; i += BX * BY) s_ops[i] = ops[i];
     __syncthreads();
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-    if (vel && x < gv.W && y < gv.H) {
-        const size_t i = (size_t)y * gv.P + x;
-        float2 a = vel[i];
-        for (int k = 0; k < n; ++k) {
-            const ForceOp& op = s_ops[k];
-            if (op.kind == FORCE_CONE_VELOCITY) {
-                const float spx = op.px * (float)gv.W, spy = op.py * (float)gv.H;
-                const float dx = spx - (float)x, dy = spy - (float)y;
-                const float len = sqrtf(dx * dx + dy * dy);
-                if (len <= op.r) {
-                    a.x = a.x + op.vx * (op.r - len) / op.r;
-                    a.y = a.y + op.vy * (op.r - len) / op.r;
-                }
-            } else if (op.kind == FORCE_GAUSS) {
-                const float cx = op.px * (float)gv.W, cy = op.py * (float)gv.H;
-                const float dx = (float)x - cx, dy = (float)y - cy;
-                const float cut = 3.0f * op.r;
-                if (dx * dx + dy * dy <= cut * cut) {
-                    const float w = nx_expf(-(dx * dx + dy * dy) / (op.r * op.r));
-                    a.x = a.x + w * op.vx;
-                    a.y = a.y + w * op.vy;
-                }
-            } else {
-                continue;
+    const int bx0 = blockIdx.x * BX, by0 = blockIdx.y * BY;
+    const int bx1 = bx0 + BX - 1, by1 = by0 + BY - 1;
+    const int x = bx0 + threadIdx.x, y = by0 + threadIdx.y;
+    if (vel) {
+        int first_vel = -1;
+        for (int k = 0; k < n; ++k)
+            if (op_is_velocity(s_ops[k].kind)) {
+                first_vel = k;
+                break;
             }
-            a.x = clampf(a.x, -1.0f, 1.0f);
-            a.y = clampf(a.y, -1.0f, 1.0f);
-        }
-        vel[i] = a;
-    }
-    if (rho && x < gd.W && y < gd.H) {
-        const size_t i = (size_t)y * gd.P + x;
-        float a = rho[i];
-        for (int k = 0; k < n; ++k) {
+        const int nk = cull_ops(n, s_kept, [&](int k) {
             const ForceOp& op = s_ops[k];
-            if (op.kind == FORCE_GAUSS) {
-                const float cx = op.px * (float)gd.W, cy = op.py * (float)gd.H;
-                const float dx = (float)x - cx, dy = (float)y - cy;
-                const float cut = 3.0f * op.r;
-                if (dx * dx + dy * dy <= cut * cut) {
-                    const float w = nx_expf(-(dx * dx + dy * dy) / (op.r * op.r));
-                    a = clampf(a + w * op.s, 0.0f, 255.0f);
+            if (op.kind == FORCE_CONE_VELOCITY)
+                return disc_meets_box(op.px * (float)gv.W, op.py * (float)gv.H, op.r, bx0, bx1,
+                                      by0, by1);
+            if (op.kind == FORCE_GAUSS)
+                return disc_meets_box(op.px * (float)gv.W, op.py * (float)gv.H, 3.0f * op.r, bx0,
+                                      bx1, by0, by1);
+            return false;
+        });
+        if (first_vel >= 0 && x < gv.W && y < gv.H) {
+            const size_t i = (size_t)y * gv.P + x;
+            float2 a = vel[i];
+            // the first velocity op culled for this block: it clamps the cell
+            bool started = !(nk > 0 && s_kept[0] == first_vel);
+            if (started) {
+                a.x = clampf(a.x, -1.0f, 1.0f);
+                a.y = clampf(a.y, -1.0f, 1.0f);
+            }
+            for (int kk = 0; kk < nk; ++kk) {
+                const ForceOp& op = s_ops[s_kept[kk]];
+                bool hit = false;
+                float ax = a.x, ay = a.y;
+                if (op.kind == FORCE_CONE_VELOCITY) {
+                    const float spx = op.px * (float)gv.W, spy = op.py * (float)gv.H;
+                    const float dx = spx - (float)x, dy = spy - (float)y;
+                    const float len = sqrtf(dx * dx + dy * dy);
+                    if (len <= op.r) {
+                        ax = a.x + op.vx * (op.r - len) / op.r;
+                        ay = a.y + op.vy * (op.r - len) / op.r;
+                        hit = true;
+                    }
+                } else {
+                    const float cx = op.px * (float)gv.W, cy = op.py * (float)gv.H;
+                    const float dx = (float)x - cx, dy = (float)y - cy;
+                    const float cut = 3.0f * op.r;
+                    if (dx * dx + dy * dy <= cut * cut) {
+                        const float w = nx_expf(-(dx * dx + dy * dy) / (op.r * op.r));
+                        ax = a.x + w * op.vx;
+                        ay = a.y + w * op.vy;
+                        hit = true;
+                    }
                 }
-            } else if (op.kind == FORCE_CONE_DENSITY) {
-                if (y < op.rows) {
+                if (hit || !started) {
+                    a.x = clampf(ax, -1.0f, 1.0f);
+                    a.y = clampf(ay, -1.0f, 1.0f);
+                    started = true;
+                }
+            }
+            vel[i] = a;
+        }
+        __syncthreads();  // s_kept is reused below
+    }
+    if (rho) {
+        const int nk = cull_ops(n, s_kept, [&](int k) {
+            const ForceOp& op = s_ops[k];
+            if (op.kind == FORCE_GAUSS)
+                return disc_meets_box(op.px * (float)gd.W, op.py * (float)gd.H, 3.0f * op.r, bx0,
+                                      bx1, by0, by1);
+            if (op.kind == FORCE_CONE_DENSITY)
+                return by0 < op.rows && disc_meets_box(op.px * (float)gd.W, op.py * (float)gd.H,
+                                                       op.r, bx0, bx1, by0, by1);
+            return false;
+        });
+        if (nk > 0 && x < gd.W && y < gd.H) {
+            const size_t i = (size_t)y * gd.P + x;
+            float a = rho[i];
+            for (int kk = 0; kk < nk; ++kk) {
+                const ForceOp& op = s_ops[s_kept[kk]];
+                if (op.kind == FORCE_GAUSS) {
+                    const float cx = op.px * (float)gd.W, cy = op.py * (float)gd.H;
+                    const float dx = (float)x - cx, dy = (float)y - cy;
+                    const float cut = 3.0f * op.r;
+                    if (dx * dx + dy * dy <= cut * cut) {
+                        const float w = nx_expf(-(dx * dx + dy * dy) / (op.r * op.r));
+                        a = clampf(a + w * op.s, 0.0f, 255.0f);
+                    }
+                } else if (y < op.rows) {
                     const float spx = op.px * (float)gd.W, spy = op.py * (float)gd.H;
                     const float dx = spx - (float)x, dy = spy - (float)y;
                     const float len = sqrtf(dx * dx + dy * dy);
                     if (len <= op.r) a = clampf(a + op.s * (op.r - len) / op.r, 0.0f, 255.0f);
                 }
             }
+            rho[i] = a;
         }
-        rho[i] = a;
     }
 }
 

@@ -353,3 +353,62 @@ def test_500_steps_512_bit_exact_and_tolerance(cuda, oracle):
             check_f64(got, ref_fields(r64, d64), step)
     den.destroy()
     sim.destroy()
+
+
+def test_forcing_order_and_clamp_edge_cases(cuda, oracle):
+    """Queued forcing is applied per cell in queue order with the reference's
+    clamp-every-cell rule, including cells whose velocity starts outside
+    [-1, 1] and are (or are not) touched by the first op."""
+    from natrix_gb300 import _lib
+
+    W, H = 96, 64
+    sim, den, ref, rden = make_pair(oracle, W, H, iterations=4, speed=5.0)
+    rng = np.random.default_rng(17)
+    v0 = rng.uniform(-3, 3, (H, W, 2)).astype(np.float32)
+    sim.upload(_lib.FIELD_VELOCITY, v0)
+    ref.vel[ref.vr][:] = v0
+    ops = [((0.2, 0.3), (0.6, -0.2), 9.0), ((0.7, 0.6), (-0.4, 0.9), 14.0),
+           ((0.22, 0.31), (0.3, 0.3), 5.0)]
+    for pos, vel, r in ops:
+        sim.add_velocity(pos, vel, r)
+        ref.add_velocity(pos, vel, r)
+    splats = np.array([[0.5, 0.5, 4.0, 0.8, -0.8, 0.5], [0.1, 0.9, 2.0, -1.0, 1.0, 1.0]],
+                      np.float32)
+    sim.add_splats(splats, den)
+    ref.add_splats(splats, rden)
+    assert_equal_f32(sim.download(_lib.FIELD_VELOCITY), ref.velocity, "forcing queue")
+    assert_equal_f32(den.download(), rden.field, "density forcing")
+    den.destroy()
+    sim.destroy()
+
+
+def test_degenerate_triangle_and_many_shapes(cuda, oracle):
+    """A zero-area triangle (the reference's same-sign test then marks every
+    cell on its line, or the whole grid when the vertices coincide) and more
+    shapes than one launch stages."""
+    from natrix_gb300 import _lib
+
+    W, H = 80, 50
+    for tri in [((0.5, 0.5), (0.5, 0.5), (0.5, 0.5)), ((0.1, 0.2), (0.3, 0.2), (0.6, 0.2))]:
+        sim, den, ref, rden = make_pair(oracle, W, H, iterations=3)
+        for s in (sim, ref):
+            s.add_triangle_obstacle(*tri, False)
+        want = np.zeros((H, W), np.uint8)
+        oracle.add_triangle_obstacle(want, *tri, False)
+        np.testing.assert_array_equal(sim.obstacles.cpu().numpy(), want)
+        den.destroy()
+        sim.destroy()
+    sim, den, ref, rden = make_pair(oracle, W, H, iterations=3)
+    rng = np.random.default_rng(2)
+    want = np.zeros((H, W), np.uint8)
+    for k in range(300):
+        px, py, r = rng.random(), rng.random(), rng.uniform(0.5, 4)
+        sim.add_circle_obstacle((px, py), r)
+        oracle.add_circle_obstacle(want, px, py, r)
+        if k % 50 == 0:
+            t = tuple(tuple(rng.random(2)) for _ in range(3))
+            sim.add_triangle_obstacle(*t, k % 100 == 0)
+            oracle.add_triangle_obstacle(want, *t, k % 100 == 0)
+    np.testing.assert_array_equal(sim.obstacles.cpu().numpy(), want)
+    den.destroy()
+    sim.destroy()
