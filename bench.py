@@ -339,12 +339,14 @@ def run_natrix(args, spec):
 
 
 def load_traffic(spec):
-    """DRAM bytes per Jacobi launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "traffic.json"
-    if p.exists():
-        d = json.loads(p.read_text())
-        return d.get(spec.name)
-    return None
+    """DRAM bytes (read + write) per Jacobi launch from the committed ncu
+    summary of this grid size (profiles/jacobi_rt_<W>x<H>.txt), if any."""
+    p = ROOT / "profiles" / f"jacobi_rt_{spec.width}x{spec.height}.txt"
+    if not p.exists():
+        return None
+    vals = [float(line.split()[-1]) for line in p.read_text().splitlines()
+            if "traffic (dram read + write) MB" in line]
+    return sum(vals) / len(vals) * 1e6 if vals else None
 
 
 def main():

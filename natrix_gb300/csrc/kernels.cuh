@@ -88,7 +88,12 @@ struct JacobiMaps {
     CUtensorMap p[2];  // pressure ping-pong buffers as sources
     CUtensorMap div;
     CUtensorMap flags;
+    int config;  // kernel configuration the boxes were encoded for
 };
+
+// Kernel configuration picked for a grid (0 = shared-memory sweeps,
+// 1 / 2 = register-tiled persistent with 112x112 / 112x128 output tiles).
+int jacobi_config(Grid g);
 
 // Largest sweep count one launch fuses (the tile halo).
 int jacobi_max_sweeps_per_launch();
