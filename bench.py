@@ -125,7 +125,8 @@ class ClockSampler:
 
 
 def make_spec(name: str) -> wl.Workload:
-    return {"large": wl.LARGE_2048, "small": wl.SMALL_256}[name]
+    return {"large": wl.LARGE_2048, "small": wl.SMALL_256,
+            "particles": wl.PARTICLES_1024}[name]
 
 
 def workload_config(spec: wl.Workload, extra=None):
@@ -349,13 +350,81 @@ def load_traffic(spec):
     return sum(vals) / len(vals) * 1e6 if vals else None
 
 
+def run_particles(args, spec):
+    """Lagrangian particles coupled to the solver: particle-steps/s of the
+    particle kernel (RK2 + 3x3 splat) and of the whole coupled frame."""
+    import torch
+
+    from natrix_gb300 import FluidSimulator
+    from natrix_gb300.core.particles import LagrangianParticles
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    W, H, n = spec.width, spec.height, wl.N_PARTICLES
+    sim = FluidSimulator(W, H)
+    sim.iterations, sim.vorticity, sim.viscosity = spec.iterations, spec.vorticity, spec.viscosity
+    sim.speed, sim.dissipation = spec.speed, spec.dissipation
+    parts = LagrangianParticles(sim, wl.uniform_particles(0, n, W, H))
+    obst = wl.workload_obstacles(0, spec)
+    forcing = [wl.step_forcing(0, i, spec) for i in range(args.warmup + args.steps)]
+    stream = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+
+    def frame(i, ev=None):
+        for o in obst:
+            sim.add_circle_obstacle((float(o[0]), float(o[1])), float(o[2]))
+        sim.add_splats(forcing[i])
+        sim.update(spec.dt)
+        if ev:
+            ev[0].record(stream)
+        parts.step(spec.dt)
+        if ev:
+            ev[1].record(stream)
+
+    for i in range(args.warmup):
+        frame(i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
+        e0.record(stream)
+        for k in range(args.steps):
+            frame(args.warmup + k, evs[k])
+        e1.record(stream)
+        torch.cuda.synchronize()
+    sim.sync()
+    frame_ms = e0.elapsed_time(e1) / args.steps
+    part_ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    peak, peak_kind = load_peaks()
+    alg = 16.0 * n + 4.0 * W * H  # positions read + write, density clear
+    line = {
+        "metric": "particle-steps/s", "value": n / (part_ms / 1e3), "unit": "particle-steps/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": part_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (uniform particles, seeded splats and discs)",
+        "config": workload_config(spec, {"particles": n}),
+        "coupled_frame": {"ms_per_step": frame_ms,
+                          "particle_steps_per_s": n / (frame_ms / 1e3),
+                          "cell_updates_per_s": W * H / (frame_ms / 1e3)},
+        "roofline": {"kernel": "particles (RK2 + 3x3 splat, red.add.f32)", "bound": "hbm",
+                     "achieved": alg / (part_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg / (part_ms / 1e3) / 1e9 / peak, "traffic": None,
+                     "peak_kind": peak_kind,
+                     "bytes_model": "16 B per particle + 4 B per density cell",
+                     "atomics_per_s": 9.0 * n / (part_ms / 1e3)},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    parts.destroy()
+    sim.destroy()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["natrix", "reference"], default="natrix")
-    ap.add_argument("--workload", choices=["large", "small"], default="large")
+    ap.add_argument("--workload", choices=["large", "small", "particles"], default="large")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "natrix":
@@ -363,6 +432,8 @@ def main():
     spec = make_spec(args.workload)
     if args.impl == "reference":
         run_reference(args, spec)
+    elif args.workload == "particles":
+        run_particles(args, spec)
     else:
         run_natrix(args, spec)
 

@@ -158,6 +158,29 @@ int natrix_density_field(natrix_density* d, void** dev_ptr, int64_t* pitch_elems
 int natrix_density_upload(natrix_density* d, const float* host, void* stream);
 int natrix_density_download(natrix_density* d, float* host, void* stream);
 
+/* --- Lagrangian particles (no reference counterpart) ---------------------
+ * Point particles moved through a simulator's velocity field by RK2
+ * (midpoint) with the bilinear sampler of shader.AdvectVelocity.comp:38-48
+ * and displacement v * dt * speed (the simulator's speed), clamped to the
+ * grid, then splatted with unit mass into a density grid of the simulator's
+ * size by a 3x3 normalised linear hat around the nearest cell centre. */
+typedef struct natrix_particles natrix_particles;
+
+/* `n` particles bound to `fluid` (positions in cells, x then y). */
+int natrix_particles_create(natrix_sim* fluid, int64_t n, natrix_particles** out);
+int natrix_particles_destroy(natrix_particles* p);
+/* Copy n float2 positions from / to host memory (stream-ordered). */
+int natrix_particles_upload(natrix_particles* p, const float* host_xy, void* stream);
+int natrix_particles_download(natrix_particles* p, float* host_xy, void* stream);
+/* One step: advect every particle; if `splat`, clear the density grid and
+ * deposit every particle into it. */
+int natrix_particles_step(natrix_particles* p, float dt, int32_t splat, void* stream);
+/* Integer cell (floor(p + 0.5) per axis) of every particle, n int2 to host. */
+int natrix_particles_cells(natrix_particles* p, int32_t* host_cells, void* stream);
+/* Device pointers of the positions (float2[n]) and the density grid (float,
+ * rows of `pitch` elements). */
+int natrix_particles_field(natrix_particles* p, void** pos, void** density, int64_t* pitch);
+
 /* Counters of one handle (and the density grids attached to it). */
 typedef struct natrix_stats {
     int64_t kernel_launches; /* kernels this library launched for the handle */

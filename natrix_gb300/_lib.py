@@ -82,6 +82,13 @@ SIGNATURES = {
     "natrix_density_field": [_vp, _vpp, _i64p],
     "natrix_density_upload": [_vp, _vp, _vp],
     "natrix_density_download": [_vp, _vp, _vp],
+    "natrix_particles_create": [_vp, ctypes.c_int64, _vpp],
+    "natrix_particles_destroy": [_vp],
+    "natrix_particles_upload": [_vp, _vp, _vp],
+    "natrix_particles_download": [_vp, _vp, _vp],
+    "natrix_particles_step": [_vp, _f, _i, _vp],
+    "natrix_particles_cells": [_vp, _vp, _vp],
+    "natrix_particles_field": [_vp, _vpp, _vpp, _i64p],
     "natrix_residual_noalloc": [_vp, _vp, _vp, _i, _i, ctypes.c_int64, _vp, _vp],
     "natrix_last_error": [],
     "natrix_version": [],

@@ -28,6 +28,7 @@ UNITS = {
     "jacobi_tma.cu": ["-fmad=false"],
     "capi.cu": [],
     "noalloc.cu": ["-fmad=false"],
+    "particles.cu": ["-fmad=false"],
 }
 
 

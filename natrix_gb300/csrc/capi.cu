@@ -44,6 +44,15 @@ int fail(int code, const char* fmt, ...) {
 
 }  // namespace
 
+// Restores the caller's current device on scope exit.
+natrix::DeviceGuard::DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+}
+natrix::DeviceGuard::~DeviceGuard() {
+    int cur;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+}
+
 int natrix::set_last_error(int code, const char* msg) {
     g_err = msg;
     return code;
@@ -67,18 +76,6 @@ int cuda_fail(cudaError_t e, const char* what) {
         NX_CUDA(call);                 \
         (sim)->stats.kernel_launches++; \
     } while (0)
-
-// Restores the caller's current device on scope exit.
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        int cur;
-        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-    }
-};
 
 int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
@@ -329,6 +326,20 @@ int materialise_mask(natrix_sim* s, cudaStream_t st) {
 }
 
 }  // namespace
+
+int natrix::sim_prepare_read(natrix_sim* s, cudaStream_t st, SimView* out) {
+    s->last_stream = st;
+    int rc = flush_fluid(s, st);
+    if (rc) return rc;
+    *out = SimView{s->vel[0], s->g, s->prm.speed, s->device};
+    return NATRIX_OK;
+}
+
+void natrix::sim_describe(const natrix_sim* s, SimView* out) {
+    *out = SimView{s->vel[0], s->g, s->prm.speed, s->device};
+}
+
+void natrix::sim_count_launches(natrix_sim* s, int n) { s->stats.kernel_launches += n; }
 
 extern "C" {
 

@@ -55,6 +55,34 @@ constexpr int kMaxOpsPerLaunch = 256;
 // Record `msg` as the calling thread's natrix_last_error() and return `code`.
 int set_last_error(int code, const char* msg);
 
+// What other translation units need of a simulator handle: its velocity
+// state buffer and geometry after every queued op has been applied.
+struct SimView {
+    const float2* vel;
+    Grid g;
+    float speed;
+    int device;
+};
+
+}  // namespace natrix
+
+struct natrix_sim;
+
+namespace natrix {
+
+// Apply the handle's queued ops on `st` and describe its velocity field.
+int sim_prepare_read(natrix_sim* sim, cudaStream_t st, SimView* out);
+// Describe the handle without launching anything.
+void sim_describe(const natrix_sim* sim, SimView* out);
+// Make `sim`'s device current for the lifetime of the guard.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev);
+    ~DeviceGuard();
+};
+// Count `n` kernel launches in the handle's statistics.
+void sim_count_launches(natrix_sim* sim, int n);
+
 // ---- per-cell kernels (solver_kernels.cu) --------------------------------
 cudaError_t launch_obstacles(uint8_t* mask, Grid g, const ShapeOp* ops, int n, int fresh,
                              cudaStream_t st);

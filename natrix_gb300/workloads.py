@@ -49,6 +49,24 @@ LARGE_2048 = Workload("plain-2048x2048-K80-eps0.35-12discs", 2048, 2048, 80, 0.3
                       0.99, 5.0, 1.0 / 60.0, 500, 16, 12)
 
 
+# Lagrangian particles: 4,194,304 particles uniform in a 1024x1024 solver with
+# the large workload's settings at 40 sweeps, 300 steps.
+PARTICLES_1024 = Workload("particles-4M-1024x1024-K40-eps0.35-12discs", 1024, 1024, 40, 0.35,
+                          0.0, 0.99, 5.0, 1.0 / 60.0, 300, 16, 12)
+N_PARTICLES = 4_194_304
+
+
+def uniform_particles(seed: int, n: int, width: int, height: int) -> np.ndarray:
+    """n float32 positions (x, y) in cells, uniform over the grid, ordered by
+    row-major cell (spatially coherent order: neighbouring threads deposit
+    into neighbouring cells)."""
+    rng = np.random.default_rng([seed, 3])
+    pos = np.stack([rng.uniform(0, width - 1, n), rng.uniform(0, height - 1, n)], 1)
+    pos = pos.astype(np.float32)
+    key = np.floor(pos[:, 1] + 0.5).astype(np.int64) * width + np.floor(pos[:, 0] + 0.5)
+    return np.ascontiguousarray(pos[np.argsort(key, kind="stable")])
+
+
 def gauss_splats(rng: np.random.Generator, n: int, width: int, height: int,
                  speed: float, radius_frac: float = 0.02,
                  amp_cells_per_s: float = 5.0) -> np.ndarray:
