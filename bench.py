@@ -418,17 +418,132 @@ def run_particles(args, spec):
     sim.destroy()
 
 
+def run_batch(args):
+    """512 independent simulations (sides 64-512, 20/40/80 sweeps, 0-6 discs,
+    8 splats each per step) in one graph launch per step, against looping
+    the single-grid simulator over the same simulations."""
+    import torch
+
+    from natrix_gb300 import FluidSimulator, SmoothParticlesArea
+    from natrix_gb300.core.batch import FluidBatch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    spec = wl.BATCH_512
+    sides, its = spec.sides(), spec.iterations()
+    n = spec.n_sims
+    total_steps = args.warmup + args.steps
+    obst = [spec.obstacles(i, int(sides[i])) for i in range(n)]
+    ocounts = np.array([len(o) for o in obst], np.int32)
+    ocat = np.concatenate([o for o in obst if len(o)] or [np.zeros((0, 3), np.float32)])
+    forcing = [np.concatenate([spec.forcing(i, k, int(sides[i])) for i in range(n)])
+               for k in range(total_steps)]
+    fcounts = np.full(n, spec.splats_per_step, np.int32)
+    batch = FluidBatch(list(sides), list(sides))
+    for i in range(n):
+        batch.set_params(i, speed=5.0, iterations=int(its[i]), dissipation=0.99, vorticity=0.0,
+                         viscosity=0.0)
+    batch.set_density_params(-1, speed=5.0, dissipation=0.99)
+    tuning = batch.autotune()
+    stream = torch.cuda.current_stream()
+
+    def frame(k):
+        batch.add_circles_bulk(ocounts, ocat)
+        batch.add_splats_bulk(fcounts, forcing[k])
+        batch.step(1 / 60)
+
+    for k in range(args.warmup):
+        frame(k)
+    batch.sync()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
+        e0.record(stream)
+        for k in range(args.warmup, total_steps):
+            frame(k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    batch.sync()
+    ms = e0.elapsed_time(e1) / args.steps
+    cells = float((sides.astype(np.float64) ** 2).sum())
+    model_bytes = float(((sides.astype(np.float64) ** 2) * (92 + 13 * its)).sum())
+    launches_total, per_step = batch.launches()
+    batch.destroy()
+
+    # looping the single-grid simulator over the same simulations
+    loop_ms = None
+    if not args.no_cpu:
+        sims = []
+        for i in range(n):
+            s = FluidSimulator(int(sides[i]), int(sides[i]))
+            d = SmoothParticlesArea(int(sides[i]), int(sides[i]), s)
+            s.speed, s.iterations, s.dissipation, s.vorticity, s.viscosity = (
+                5.0, int(its[i]), 0.99, 0.0, 0.0)
+            d.speed, d.dissipation = 5.0, 0.99
+            sims.append((s, d))
+        loop_steps = 3
+        off = np.concatenate([[0], np.cumsum(fcounts)])
+
+        def loop_frame(k):
+            f = forcing[k]
+            for i, (s, d) in enumerate(sims):
+                for o in obst[i]:
+                    s.add_circle_obstacle((float(o[0]), float(o[1])), float(o[2]))
+                s.add_splats(f[off[i]:off[i + 1]], d)
+                s.update(1 / 60)
+                d.update(1 / 60)
+
+        loop_frame(0)
+        torch.cuda.synchronize()
+        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0.record(stream)
+        for k in range(1, 1 + loop_steps):
+            loop_frame(k)
+        l1.record(stream)
+        torch.cuda.synchronize()
+        loop_ms = l0.elapsed_time(l1) / loop_steps
+        for s, d in sims:
+            d.destroy()
+            s.destroy()
+    peak, peak_kind = load_peaks()
+    line = {
+        "metric": "cell-updates/s", "value": cells / (ms / 1e3), "unit": "cell-updates/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded sides, sweeps, discs and splats)",
+        "config": {"workload": spec.name, "simulations": n, "cells": cells,
+                   "sides": [int(sides.min()), int(sides.max())],
+                   "jacobi_sweeps": {str(k): int((its == k).sum()) for k in (20, 40, 80)},
+                   "tuning": {wl_name: list(v) for wl_name, v in
+                              zip(("side<=128", "side<=256", "side>256"),
+                                  [tuning.get(c, (None, None)) for c in range(3)])}},
+        "hbm_roofline_model": {"bytes_per_step": model_bytes,
+                               "achieved_gbs": model_bytes / (ms / 1e3) / 1e9,
+                               "frac": model_bytes / (ms / 1e3) / 1e9 / peak, "peak_gbs": peak,
+                               "peak_kind": peak_kind},
+        "gpu_launches_per_step": per_step,
+        "looped_single_grid": None if loop_ms is None else {
+            "ms_per_step": loop_ms, "value": cells / (loop_ms / 1e3),
+            "speedup_of_batch": loop_ms / ms},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["natrix", "reference"], default="natrix")
-    ap.add_argument("--workload", choices=["large", "small", "particles"], default="large")
+    ap.add_argument("--workload", choices=["large", "small", "particles", "batch"],
+                    default="large")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "natrix":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.workload == "batch":
+        run_batch(args)
+        return
     spec = make_spec(args.workload)
     if args.impl == "reference":
         run_reference(args, spec)

@@ -58,7 +58,8 @@ enum natrix_field_id {
     NATRIX_FIELD_PRESSURE = 1,   /* float  [H][pitch]; pressure after the last step's sweeps */
     NATRIX_FIELD_DIVERGENCE = 2, /* float  [H][pitch] */
     NATRIX_FIELD_VORTICITY = 3,  /* float  [H][pitch] */
-    NATRIX_FIELD_OBSTACLES = 4   /* uint8  [H][pitch]; bit0 = obstacle (x), bit1 = static triangle (y) */
+    NATRIX_FIELD_OBSTACLES = 4,  /* uint8  [H][pitch]; bit0 = obstacle (x), bit1 = static triangle (y) */
+    NATRIX_FIELD_DENSITY = 5     /* float  [H][pitch]; batches only (density grid of each simulation) */
 };
 
 /* Number of floats per splat record passed to natrix_add_splats. */
@@ -180,6 +181,52 @@ int natrix_particles_cells(natrix_particles* p, int32_t* host_cells, void* strea
 /* Device pointers of the positions (float2[n]) and the density grid (float,
  * rows of `pitch` elements). */
 int natrix_particles_field(natrix_particles* p, void** pos, void** density, int64_t* pitch);
+
+/* --- batches of independent simulations (no reference counterpart) -------
+ * n simulations of their own sizes, each a FluidSimulator with a density grid
+ * of the same size (SmoothParticlesArea), advanced together: one launch per
+ * phase covers every simulation and the whole step is captured once as a
+ * CUDA graph and replayed.  Each simulation gives the same result, bit for
+ * bit, as a single simulator stepped through the same calls (obstacles are
+ * discs; forcing is add_velocity cones and Gaussian splats on velocity and
+ * density). */
+typedef struct natrix_batch natrix_batch;
+
+int natrix_batch_create(int32_t n, const int32_t* widths, const int32_t* heights,
+                        natrix_batch** out);
+int natrix_batch_destroy(natrix_batch* b);
+/* Parameters of simulation `sim` (-1 = all); validation as natrix_set_params. */
+int natrix_batch_set_params(natrix_batch* b, int32_t sim, const natrix_params* p);
+int natrix_batch_set_density_params(natrix_batch* b, int32_t sim, float speed,
+                                    float dissipation);
+/* Jacobi tile configuration (0 = 64x32 shared-memory tiles, 1 = 112x112 and
+ * 2 = 112x128 register tiles) and sweeps per launch (1..8) for a size class
+ * (0: side <= 128, 1: <= 256, 2: larger). */
+int natrix_batch_set_tuning(natrix_batch* b, int32_t size_class, int32_t config,
+                            int32_t sweeps_per_launch);
+/* Replay a captured CUDA graph per step (default 1) or launch directly (0). */
+int natrix_batch_set_graph(natrix_batch* b, int32_t enable);
+/* Queued per simulation for the next step (at most 256 ops and 256 shapes
+ * per simulation per step, else NATRIX_ERANGE). */
+int natrix_batch_add_velocity(natrix_batch* b, int32_t sim, float px, float py, float vx,
+                              float vy, float radius);
+int natrix_batch_add_splats(natrix_batch* b, int32_t sim, const float* splats, int32_t n);
+int natrix_batch_add_circle_obstacle(natrix_batch* b, int32_t sim, float px, float py,
+                                     float radius, int32_t is_static);
+/* The same for every simulation at once: counts[n] records per simulation,
+ * records concatenated in simulation order (splats: NATRIX_SPLAT_FLOATS
+ * floats each; circles: px, py, radius). */
+int natrix_batch_add_splats_bulk(natrix_batch* b, const int32_t* counts, const float* splats);
+int natrix_batch_add_circles_bulk(natrix_batch* b, const int32_t* counts, const float* circles);
+/* One step of every simulation (fluid update, then density update). */
+int natrix_batch_step(natrix_batch* b, float dt, void* stream);
+int natrix_batch_field(natrix_batch* b, int32_t sim, int32_t field, void** dev_ptr,
+                       int64_t* pitch_elems);
+int natrix_batch_download(natrix_batch* b, int32_t sim, int32_t field, void* host,
+                          void* stream);
+/* Kernels launched so far and per step. */
+int natrix_batch_launches(natrix_batch* b, int64_t* total, int32_t* per_step);
+int natrix_batch_sync(natrix_batch* b, void* stream);
 
 /* Counters of one handle (and the density grids attached to it). */
 typedef struct natrix_stats {

@@ -23,6 +23,7 @@ FIELD_PRESSURE = 1
 FIELD_DIVERGENCE = 2
 FIELD_VORTICITY = 3
 FIELD_OBSTACLES = 4
+FIELD_DENSITY = 5
 
 SPLAT_FLOATS = 6
 
@@ -89,6 +90,22 @@ SIGNATURES = {
     "natrix_particles_step": [_vp, _f, _i, _vp],
     "natrix_particles_cells": [_vp, _vp, _vp],
     "natrix_particles_field": [_vp, _vpp, _vpp, _i64p],
+    "natrix_batch_create": [_i, _vp, _vp, _vpp],
+    "natrix_batch_destroy": [_vp],
+    "natrix_batch_set_params": [_vp, _i, ctypes.POINTER(Params)],
+    "natrix_batch_set_density_params": [_vp, _i, _f, _f],
+    "natrix_batch_set_tuning": [_vp, _i, _i, _i],
+    "natrix_batch_set_graph": [_vp, _i],
+    "natrix_batch_add_velocity": [_vp, _i, _f, _f, _f, _f, _f],
+    "natrix_batch_add_splats": [_vp, _i, _vp, _i],
+    "natrix_batch_add_circle_obstacle": [_vp, _i, _f, _f, _f, _i],
+    "natrix_batch_add_splats_bulk": [_vp, _vp, _vp],
+    "natrix_batch_add_circles_bulk": [_vp, _vp, _vp],
+    "natrix_batch_step": [_vp, _f, _vp],
+    "natrix_batch_field": [_vp, _i, _i, _vpp, _i64p],
+    "natrix_batch_download": [_vp, _i, _i, _vp, _vp],
+    "natrix_batch_launches": [_vp, _i64p, ctypes.POINTER(ctypes.c_int32)],
+    "natrix_batch_sync": [_vp, _vp],
     "natrix_residual_noalloc": [_vp, _vp, _vp, _i, _i, ctypes.c_int64, _vp, _vp],
     "natrix_last_error": [],
     "natrix_version": [],

@@ -29,6 +29,7 @@ UNITS = {
     "capi.cu": [],
     "noalloc.cu": ["-fmad=false"],
     "particles.cu": ["-fmad=false"],
+    "batch.cu": ["-fmad=false"],
 }
 
 

@@ -83,7 +83,7 @@ int round_up(int v, int m) { return (v + m - 1) / m * m; }
 // Each slot is reused only after the copy that last read it has completed.
 struct UploadRing {
     static constexpr int kSlots = 8;
-    static constexpr size_t kSlotBytes = 64 * 1024;
+    static constexpr size_t kSlotBytes = 16 * 1024;  // >= 256 ops of 32 bytes
     unsigned char* host = nullptr;
     cudaEvent_t ev[kSlots] = {};
     int next = 0;
@@ -137,7 +137,8 @@ struct natrix_sim {
     double* d_res = nullptr;  // partials, then the 5 sums at the end
     double* h_res = nullptr;  // pinned
     int res_blocks = 0;
-    JacobiMaps maps{};
+    JacobiMaps maps{};             // host copy (encoded at creation)
+    JacobiMaps* d_maps = nullptr;  // device copy the sweep kernels read
     UploadRing ring;
     std::vector<ForceOp> fq;
     std::vector<ShapeOp> sq;
@@ -191,6 +192,7 @@ void free_sim(natrix_sim* s) {
     cudaFree(s->d_shape);
     cudaFree(s->d_status);
     cudaFree(s->d_res);
+    cudaFree(s->d_maps);
     if (s->h_res) cudaFreeHost(s->h_res);
     s->ring.release();
     delete s;
@@ -272,7 +274,8 @@ int run_jacobi(natrix_sim* s, int sweeps, cudaStream_t st) {
     int launches = 0, total = sweeps;
     while (sweeps > 0) {
         const int k = sweeps < per ? sweeps : per;
-        NX_LAUNCH(s, launch_jacobi(s->maps, s->p, s->p_cur, s->g, k, s->d_status, st));
+        NX_LAUNCH(s, launch_jacobi(s->d_maps, s->maps.config, s->p, s->p_cur, s->g, k,
+                                   s->d_status, st));
         s->p_cur ^= 1;
         sweeps -= k;
         ++launches;
@@ -391,9 +394,17 @@ int natrix_create(int32_t width, int32_t height, natrix_sim** out) {
     }
     s->mask_reset_pending = false;  // the memset left a valid empty mask
     const char* err = nullptr;
-    if (!jacobi_encode_maps(&s->maps, s->p[0], s->p[1], s->div, s->flags, s->g, &err)) {
+    if (!jacobi_encode_maps_for(&s->maps, jacobi_config(s->g), s->p[0], s->p[1], s->div,
+                                s->flags, s->g, &err)) {
         free_sim(s);
         return fail(NATRIX_ECUDA, "%s", err);
+    }
+    e = cudaMalloc(&s->d_maps, sizeof(JacobiMaps));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(s->d_maps, &s->maps, sizeof(JacobiMaps), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        free_sim(s);
+        return fail(NATRIX_ECUDA, "uploading tensor maps: %s", cudaGetErrorString(e));
     }
     *out = s;
     return NATRIX_OK;

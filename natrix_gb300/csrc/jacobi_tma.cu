@@ -1,24 +1,27 @@
 // Plain Jacobi pressure sweeps (shader.Poisson.comp:17-38, looped K times by
-// natrix/core/fluid_simulator.py:251-255), temporally blocked.
-//
-// One CTA owns a TX x TY output tile.  A single elected thread issues three
-// TMA tile loads (cp.async.bulk.tensor.2d) of the tile plus a halo of HALO
-// cells: pressure and divergence (float, x-halo rounded up to 4 cells so the
-// box starts on a 16-byte boundary) and the neighbour-substitution flags
-// (uint8, x-halo 16 for the same reason), completing on one mbarrier.  The
-// CTA then runs `sweeps` <= HALO sweeps in shared memory, ping-ponging
-// between two pressure buffers on a region that shrinks by one cell per
-// sweep, and writes the tile interior back with 16-byte stores.  Every sweep
+// natrix/core/fluid_simulator.py:251-255), temporally blocked: one launch runs
+// up to HALO sweeps on tiles loaded with a HALO-cell halo by TMA
+// (cp.async.bulk.tensor.2d) and writes only the tile interior.  Every sweep
 // evaluates exactly the reference's expression
 //     p' = (pL + pR + pB + pT - b) * 0.25
+// (neighbour replaced by the centre when it is an obstacle or beyond a wall)
 // on the same inputs, so k fused sweeps equal k single sweeps bit for bit.
 //
-// TMA fills out-of-grid cells with zeros.  No in-grid cell ever reads them:
-// a cell on a wall has the wall bit in its flags and substitutes its own
-// pressure (the clamped neighbour index of common.sh:9-19 is the cell).
-// Out-of-grid halo cells compute values nobody reads.
+// TMA boxes: pressure and divergence (float) start HXP = round_up(HALO, 4)
+// cells left of the tile so the box starts on a 16-byte boundary; the uint8
+// neighbour flags start 16 cells left for the same reason.  TMA fills
+// out-of-grid cells with zeros.  No in-grid cell ever reads them: a cell on a
+// wall has the wall bit in its flags and substitutes its own pressure (the
+// clamped neighbour index of common.sh:9-19 is the cell itself).
 //
-// The mbarrier wait is bounded; on time-out the kernel records status bit 1,
+// Two tile kernels, each templated on a job source so the same body serves
+// one grid and a batch of simulations (one work item per tile); tensor maps
+// live in device memory:
+//   * k_jacobi_rt: register tiled, persistent, next tile prefetched by TMA
+//     while the current one sweeps (grids wider than ~100 cells);
+//   * k_jacobi_tb: shared-memory sweeps on a shrinking region, one tile per
+//     CTA, several CTAs per SM (narrow grids).
+// Every mbarrier wait is bounded; on time-out the kernel records status bit 1,
 // waits once more (bounded) for its copies, and returns without writing.
 #include <cudaTypedefs.h>
 
@@ -32,26 +35,6 @@ namespace {
 
 constexpr int align128(int b) { return (b + 127) / 128 * 128; }
 
-template <int TX_, int TY_, int HALO_>
-struct JacCfg {
-    static constexpr int TX = TX_, TY = TY_, HALO = HALO_;
-    static constexpr int HXP = (HALO + 3) / 4 * 4;  // x-halo of the float boxes
-    static constexpr int HXF = 16;                    // x-halo of the uint8 box
-    static constexpr int RX = TX + 2 * HXP, RY = TY + 2 * HALO, RXF = TX + 2 * HXF;
-    static constexpr int P_BYTES = RX * RY * 4, F_BYTES = RXF * RY;
-    static constexpr int OFF_A = 0;
-    static constexpr int OFF_B = OFF_A + align128(P_BYTES);
-    static constexpr int OFF_D = OFF_B + align128(P_BYTES);
-    static constexpr int OFF_F = OFF_D + align128(P_BYTES);
-    static constexpr int OFF_BAR = OFF_F + align128(F_BYTES);
-    static constexpr int SMEM = OFF_BAR + 128;
-    static constexpr int THREADS_X = 32, THREADS_Y = 8;
-    static_assert(TX % 16 == 0, "tile width must keep the uint8 box 16-byte aligned");
-    static_assert(RX <= 256 && RY <= 256 && RXF <= 256, "TMA box dimensions are <= 256");
-};
-
-using Cfg = JacCfg<64, 32, 8>;
-
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -63,6 +46,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 
 __device__ __forceinline__ void fence_barrier_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
@@ -93,53 +80,114 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
-// Bounded wait for phase 0 of the tile barrier (about 4M polls).
-__device__ __forceinline__ bool wait_tile(uint64_t* bar) {
+// Bounded wait for the given phase parity of a tile barrier (about 4M polls).
+__device__ __forceinline__ bool wait_phase(uint64_t* bar, uint32_t parity) {
     for (int it = 0; it < (1 << 22); ++it)
-        if (mbar_try_wait(bar, 0)) return true;
+        if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
 
-__global__ void __launch_bounds__(Cfg::THREADS_X* Cfg::THREADS_Y)
-    k_jacobi_tb(const __grid_constant__ CUtensorMap tm_p, const __grid_constant__ CUtensorMap tm_div,
-                const __grid_constant__ CUtensorMap tm_flags, float* __restrict__ pout, Grid g,
-                int sweeps, int* __restrict__ status) {
+// One tile of work: where to load it from, where to write it, how far to go.
+struct TileJob {
+    const CUtensorMap* p;
+    const CUtensorMap* d;
+    const CUtensorMap* f;
+    float* pout;
+    Grid g;
+    int sweeps;
+    int tile_x, tile_y;
+};
+
+// Jobs of one grid: tile t of a tiles_x-wide decomposition.
+struct GridJobs {
+    const CUtensorMap* p;
+    const CUtensorMap* d;
+    const CUtensorMap* f;
+    float* pout;
+    Grid g;
+    int sweeps, tiles_x, n, tx, ty;
+    __device__ __forceinline__ TileJob operator()(int t) const {
+        return TileJob{p, d, f, pout, g, sweeps, (t % tiles_x) * tx, (t / tiles_x) * ty};
+    }
+};
+
+// Jobs of a batch: item t names a simulation, a tile origin, a sweep count
+// and the source pressure buffer.
+struct BatchJobs {
+    const JacobiBatchItem* items;
+    const JacobiBatchSim* sims;
+    int n;
+    __device__ __forceinline__ TileJob operator()(int t) const {
+        const JacobiBatchItem it = items[t];
+        const JacobiBatchSim& s = sims[it.sim];
+        return TileJob{&s.maps.p[it.src], &s.maps.div, &s.maps.flags, s.p[1 - it.src], s.g,
+                       it.sweeps, it.tile_x, it.tile_y};
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Shared-memory variant: TX x TY output tile, region shrinking one cell per
+// sweep, ping-pong between two pressure buffers in shared memory.
+template <int TX_, int TY_, int HALO_>
+struct TbCfg {
+    static constexpr int TX = TX_, TY = TY_, HALO = HALO_;
+    static constexpr int HXP = (HALO + 3) / 4 * 4;  // x-halo of the float boxes
+    static constexpr int HXF = 16;                    // x-halo of the uint8 box
+    static constexpr int RX = TX + 2 * HXP, RY = TY + 2 * HALO, RXF = TX + 2 * HXF;
+    static constexpr int P_BYTES = RX * RY * 4, F_BYTES = RXF * RY;
+    static constexpr int OFF_A = 0;
+    static constexpr int OFF_B = OFF_A + align128(P_BYTES);
+    static constexpr int OFF_D = OFF_B + align128(P_BYTES);
+    static constexpr int OFF_F = OFF_D + align128(P_BYTES);
+    static constexpr int OFF_BAR = OFF_F + align128(F_BYTES);
+    static constexpr int SMEM = OFF_BAR + 128;
+    static constexpr int THREADS_X = 32, THREADS_Y = 8;
+    static_assert(TX % 16 == 0, "tile width must keep the uint8 box 16-byte aligned");
+    static_assert(RX <= 256 && RY <= 256 && RXF <= 256, "TMA box dimensions are <= 256");
+};
+
+using Tb = TbCfg<64, 32, 8>;
+
+template <class C, class Jobs>
+__global__ void __launch_bounds__(C::THREADS_X* C::THREADS_Y)
+    k_jacobi_tb(const Jobs jobs, int* __restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
-    float* A = reinterpret_cast<float*>(smem + Cfg::OFF_A);
-    float* B = reinterpret_cast<float*>(smem + Cfg::OFF_B);
-    const float* D = reinterpret_cast<const float*>(smem + Cfg::OFF_D);
-    const uint8_t* F = reinterpret_cast<const uint8_t*>(smem + Cfg::OFF_F);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Cfg::OFF_BAR);
+    float* A = reinterpret_cast<float*>(smem + C::OFF_A);
+    float* B = reinterpret_cast<float*>(smem + C::OFF_B);
+    const float* D = reinterpret_cast<const float*>(smem + C::OFF_D);
+    const uint8_t* F = reinterpret_cast<const uint8_t*>(smem + C::OFF_F);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
     __shared__ int s_ok;
 
-    const int tile_x = blockIdx.x * Cfg::TX, tile_y = blockIdx.y * Cfg::TY;
+    const TileJob job = jobs(blockIdx.x);
+    const int tile_x = job.tile_x, tile_y = job.tile_y, sweeps = job.sweeps;
     const int tx = threadIdx.x, ty = threadIdx.y;
     if (tx == 0 && ty == 0) {
         mbar_init(bar, 1);
         fence_barrier_init();
-        mbar_expect_tx(bar, 2 * Cfg::P_BYTES + Cfg::F_BYTES);
-        tma_load_2d(A, &tm_p, tile_x - Cfg::HXP, tile_y - Cfg::HALO, bar);
-        tma_load_2d(smem + Cfg::OFF_D, &tm_div, tile_x - Cfg::HXP, tile_y - Cfg::HALO, bar);
-        tma_load_2d(smem + Cfg::OFF_F, &tm_flags, tile_x - Cfg::HXF, tile_y - Cfg::HALO, bar);
-        bool ok = wait_tile(bar);
+        mbar_expect_tx(bar, 2 * C::P_BYTES + C::F_BYTES);
+        tma_load_2d(A, job.p, tile_x - C::HXP, tile_y - C::HALO, bar);
+        tma_load_2d(smem + C::OFF_D, job.d, tile_x - C::HXP, tile_y - C::HALO, bar);
+        tma_load_2d(smem + C::OFF_F, job.f, tile_x - C::HXF, tile_y - C::HALO, bar);
+        bool ok = wait_phase(bar, 0);
         if (!ok) {
             atomicOr(status, 1);
-            wait_tile(bar);  // let the copies land before the CTA exits
+            wait_phase(bar, 0);  // let the copies land before the CTA exits
         }
         s_ok = ok ? 1 : 0;
     }
     __syncthreads();
     if (!s_ok) return;
 
-    constexpr int RX = Cfg::RX, RXF = Cfg::RXF, FOFF = Cfg::HXF - Cfg::HXP;
+    constexpr int RX = C::RX, RXF = C::RXF, FOFF = C::HXF - C::HXP;
     for (int s = 1; s <= sweeps; ++s) {
         const float* src = (s & 1) ? A : B;
         float* dst = (s & 1) ? B : A;
         const int m = sweeps - s;
-        const int x0 = Cfg::HXP - m, x1 = Cfg::HXP + Cfg::TX + m;
-        const int y0 = Cfg::HALO - m, y1 = Cfg::HALO + Cfg::TY + m;
-        for (int yy = y0 + ty; yy < y1; yy += Cfg::THREADS_Y) {
-            for (int xx = x0 + tx; xx < x1; xx += Cfg::THREADS_X) {
+        const int x0 = C::HXP - m, x1 = C::HXP + C::TX + m;
+        const int y0 = C::HALO - m, y1 = C::HALO + C::TY + m;
+        for (int yy = y0 + ty; yy < y1; yy += C::THREADS_Y) {
+            for (int xx = x0 + tx; xx < x1; xx += C::THREADS_X) {
                 const int i = yy * RX + xx;
                 const float pc = src[i];
                 const uint8_t f = F[yy * RXF + xx + FOFF];
@@ -156,36 +204,36 @@ __global__ void __launch_bounds__(Cfg::THREADS_X* Cfg::THREADS_Y)
 
     // tile interior -> global, 16-byte stores; a float4 group starting inside
     // the row stays inside the padded pitch (pitch and tile_x are multiples of 4)
-    constexpr int GROUPS = Cfg::TX / 4;
-    for (int k = ty * Cfg::THREADS_X + tx; k < Cfg::TY * GROUPS;
-         k += Cfg::THREADS_X * Cfg::THREADS_Y) {
+    constexpr int GROUPS = C::TX / 4;
+    const Grid& g = job.g;
+    for (int k = ty * C::THREADS_X + tx; k < C::TY * GROUPS; k += C::THREADS_X * C::THREADS_Y) {
         const int row = k / GROUPS, grp = k % GROUPS;
         const int gy = tile_y + row, gx = tile_x + grp * 4;
         if (gy >= g.H || gx >= g.W) continue;
         const float4 v =
-            *reinterpret_cast<const float4*>(res + (Cfg::HALO + row) * RX + Cfg::HXP + grp * 4);
-        *reinterpret_cast<float4*>(pout + (size_t)gy * g.P + gx) = v;
+            *reinterpret_cast<const float4*>(res + (C::HALO + row) * RX + C::HXP + grp * 4);
+        *reinterpret_cast<float4*>(job.pout + (size_t)gy * g.P + gx) = v;
     }
 }
 
 // ---------------------------------------------------------------------------
-// Register-tiled, persistent variant (the default).  The CTA region is 128
-// columns x NW*R rows; warp w owns rows [w*R, w*R + R), lane l owns columns
-// [4l, 4l + 4), so each cell of the region lives in one thread's registers
-// (pressure, divergence, flags) for all the launch's sweeps.  Per sweep a
-// thread needs, per row, its left/right neighbours (warp shuffles of the
-// adjacent lanes' edge columns) and the rows above/below (its own registers,
-// or the neighbouring warps' edge rows exchanged through a double-buffered
+// Register-tiled, persistent variant.  The CTA region is 128 columns x NW*R
+// rows; warp w owns rows [w*R, w*R + R), lane l owns columns [4l, 4l + 4), so
+// each cell of the region lives in one thread's registers (pressure,
+// divergence, flags) for all the launch's sweeps.  Per sweep a thread needs,
+// per row, its left/right neighbours (warp shuffles of the adjacent lanes'
+// edge columns) and the rows above/below (its own registers, or the
+// neighbouring warps' edge rows exchanged through a double-buffered
 // shared-memory slot: one barrier per sweep).  Rows whose warp holds no wall
 // or obstacle neighbour take a substitution-free path (warp-uniform branch).
 // Cells near the region edge compute from missing neighbours; after s sweeps
 // the outer s rows / columns are invalid and the output tile (HALO rows and
 // HXP columns in) stays exact for s <= HALO.
 //
-// The grid is persistent (one CTA per SM, tiles assigned round-robin): once
+// The grid is persistent (one CTA per SM, jobs assigned round-robin): once
 // every thread has copied the current tile's staging buffers into registers,
-// the elected thread issues the TMA loads of the CTA's next tile into the
-// same staging buffers, so the copy overlaps this tile's sweeps.
+// the elected thread issues the TMA loads of the CTA's next job into the same
+// staging buffers, so the copy overlaps this tile's sweeps.
 template <int R_, int NW_, int HALO_>
 struct RtCfg {
     static constexpr int R = R_, NW = NW_, HALO = HALO_;
@@ -213,34 +261,18 @@ using RtA = RtCfg<8, 16, 8>;
 // 16 warps x 9 rows: 128x144 region, 112x128 output tile
 using RtB = RtCfg<9, 16, 8>;
 
-__device__ __forceinline__ void fence_proxy_async() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-// Bounded wait for the given phase parity of the tile barrier.
-__device__ __forceinline__ bool wait_phase(uint64_t* bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 22); ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
 template <class C>
 __device__ __forceinline__ void issue_tile_loads(unsigned char* smem, uint64_t* bar,
-                                                 const CUtensorMap* tm_p,
-                                                 const CUtensorMap* tm_div,
-                                                 const CUtensorMap* tm_flags, int tile_x,
-                                                 int tile_y) {
+                                                 const TileJob& job) {
     mbar_expect_tx(bar, 2 * C::P_BYTES + C::F_BYTES);
-    tma_load_2d(smem + C::OFF_P, tm_p, tile_x - C::HXP, tile_y - C::HALO, bar);
-    tma_load_2d(smem + C::OFF_D, tm_div, tile_x - C::HXP, tile_y - C::HALO, bar);
-    tma_load_2d(smem + C::OFF_F, tm_flags, tile_x - C::HXF, tile_y - C::HALO, bar);
+    tma_load_2d(smem + C::OFF_P, job.p, job.tile_x - C::HXP, job.tile_y - C::HALO, bar);
+    tma_load_2d(smem + C::OFF_D, job.d, job.tile_x - C::HXP, job.tile_y - C::HALO, bar);
+    tma_load_2d(smem + C::OFF_F, job.f, job.tile_x - C::HXF, job.tile_y - C::HALO, bar);
 }
 
-template <class C>
+template <class C, class Jobs>
 __global__ void __launch_bounds__(C::THREADS, 1)
-    k_jacobi_rt(const __grid_constant__ CUtensorMap tm_p, const __grid_constant__ CUtensorMap tm_div,
-                const __grid_constant__ CUtensorMap tm_flags, float* __restrict__ pout, Grid g,
-                int sweeps, int tiles_x, int n_tiles, int* __restrict__ status) {
+    k_jacobi_rt(const Jobs jobs, int* __restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const float* Ps = reinterpret_cast<const float*>(smem + C::OFF_P);
     const float* Ds = reinterpret_cast<const float*>(smem + C::OFF_D);
@@ -254,17 +286,16 @@ __global__ void __launch_bounds__(C::THREADS, 1)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int c0 = lane * 4, r0 = w * R;
 
-    int tile = blockIdx.x;
-    if (tile >= n_tiles) return;
+    int t = blockIdx.x;
+    if (t >= jobs.n) return;
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
         fence_barrier_init();
-        issue_tile_loads<C>(smem, bar, &tm_p, &tm_div, &tm_flags, (tile % tiles_x) * C::TX,
-                            (tile / tiles_x) * C::TY);
+        issue_tile_loads<C>(smem, bar, jobs(t));
     }
     uint32_t parity = 0;
-    for (; tile < n_tiles; tile += gridDim.x, parity ^= 1u) {
-        const int tile_x = (tile % tiles_x) * C::TX, tile_y = (tile / tiles_x) * C::TY;
+    for (; t < jobs.n; t += gridDim.x, parity ^= 1u) {
+        const TileJob job = jobs(t);
         if (threadIdx.x == 0) {
             bool ok = wait_phase(bar, parity);
             if (!ok) {
@@ -289,15 +320,13 @@ __global__ void __launch_bounds__(C::THREADS, 1)
                                                       (C::HXF - C::HXP));
             if (__any_sync(FULL, f[r] != 0u)) slow |= 1u << r;
         }
-        __syncthreads();  // staging consumed: prefetch the next tile into it
-        const int next = tile + gridDim.x;
-        if (threadIdx.x == 0 && next < n_tiles) {
+        __syncthreads();  // staging consumed: prefetch the next job into it
+        if (threadIdx.x == 0 && t + (int)gridDim.x < jobs.n) {
             fence_proxy_async();
-            issue_tile_loads<C>(smem, bar, &tm_p, &tm_div, &tm_flags, (next % tiles_x) * C::TX,
-                                (next / tiles_x) * C::TY);
+            issue_tile_loads<C>(smem, bar, jobs(t + gridDim.x));
         }
 
-        for (int s = 0; s < sweeps; ++s) {
+        for (int s = 0; s < job.sweeps; ++s) {
             float* xs = X + (s & 1) * (C::NW * 2 * RX);
             *reinterpret_cast<float4*>(xs + (w * 2 + 0) * RX + c0) =
                 make_float4(p[0][0], p[0][1], p[0][2], p[0][3]);
@@ -335,8 +364,8 @@ __global__ void __launch_bounds__(C::THREADS, 1)
                         const float l = (fb & NB_L) ? cur[j] : L[j];
                         const float rr = (fb & NB_R) ? cur[j] : Rn[j];
                         const float b = (fb & NB_B) ? cur[j] : up[j];
-                        const float t = (fb & NB_T) ? cur[j] : dn[j];
-                        p[r][j] = (l + rr + b + t - d[r][j]) * 0.25f;
+                        const float tt = (fb & NB_T) ? cur[j] : dn[j];
+                        p[r][j] = (l + rr + b + tt - d[r][j]) * 0.25f;
                     }
                 } else {
 #pragma unroll
@@ -349,14 +378,15 @@ __global__ void __launch_bounds__(C::THREADS, 1)
         }
 
         // output tile: region rows [HALO, HALO + TY), columns [HXP, HXP + TX)
+        const Grid& g = job.g;
         if (c0 >= C::HXP && c0 < C::HXP + C::TX) {
-            const int gx = tile_x + c0 - C::HXP;
+            const int gx = job.tile_x + c0 - C::HXP;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int rr = r0 + r;
-                const int gy = tile_y + rr - C::HALO;
+                const int gy = job.tile_y + rr - C::HALO;
                 if (rr >= C::HALO && rr < C::HALO + C::TY && gy < g.H && gx < g.W)
-                    *reinterpret_cast<float4*>(pout + (size_t)gy * g.P + gx) =
+                    *reinterpret_cast<float4*>(job.pout + (size_t)gy * g.P + gx) =
                         make_float4(p[r][0], p[r][1], p[r][2], p[r][3]);
             }
         }
@@ -397,16 +427,16 @@ bool encode_2d(CUtensorMap* map, CUtensorMapDataType dt, int elem_bytes, void* b
     return true;
 }
 
-// Kernel variant: 0 = shared-memory sweeps (k_jacobi_tb), 1 = register tiled
-// persistent (k_jacobi_rt, default).  NATRIX_JACOBI_VARIANT selects one for
-// comparison.
-int variant() {
+// NATRIX_JACOBI_VARIANT=0 forces the shared-memory kernel on every single
+// grid (for comparison runs); otherwise the tile shape is chosen by
+// jacobi_config.
+bool force_tb() {
     static int v = -1;
     if (v < 0) {
         const char* e = getenv("NATRIX_JACOBI_VARIANT");
-        v = (e && e[0] == '0') ? 0 : 1;
+        v = (e && e[0] == '0') ? 1 : 0;
     }
-    return v;
+    return v == 1;
 }
 
 int num_sms() {
@@ -430,65 +460,99 @@ double rt_cost(Grid g) {
     return (double)rounds * C::RX * C::RY * (tiles < sms ? (double)tiles / sms : 1.0);
 }
 
-template <class C>
-cudaError_t launch_rt(const JacobiMaps& maps, float* const pbuf[2], int src, Grid g, int sweeps,
-                      int* status, cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_jacobi_rt<C>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+template <class K>
+cudaError_t set_smem(K kernel, int bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+template <class C, class Jobs>
+cudaError_t launch_rt_jobs(const Jobs& jobs, int* status, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = set_smem(k_jacobi_rt<C, Jobs>, C::SMEM);
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        attr = true;
     }
-    const int tiles_x = (g.W + C::TX - 1) / C::TX, tiles_y = (g.H + C::TY - 1) / C::TY;
-    const int n_tiles = tiles_x * tiles_y;
-    const int grid = n_tiles < num_sms() ? n_tiles : num_sms();
-    k_jacobi_rt<C><<<grid, C::THREADS, C::SMEM, st>>>(maps.p[src], maps.div, maps.flags,
-                                                      pbuf[1 - src], g, sweeps, tiles_x, n_tiles,
-                                                      status);
+    if (jobs.n == 0) return cudaSuccess;
+    const int grid = jobs.n < num_sms() ? jobs.n : num_sms();
+    k_jacobi_rt<C, Jobs><<<grid, C::THREADS, C::SMEM, st>>>(jobs, status);
     return cudaGetLastError();
+}
+
+template <class C, class Jobs>
+cudaError_t launch_tb_jobs(const Jobs& jobs, int* status, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = set_smem(k_jacobi_tb<C, Jobs>, C::SMEM);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    if (jobs.n == 0) return cudaSuccess;
+    k_jacobi_tb<C, Jobs><<<jobs.n, dim3(C::THREADS_X, C::THREADS_Y), C::SMEM, st>>>(jobs, status);
+    return cudaGetLastError();
+}
+
+template <class C>
+void box_of(int* bx, int* by, int* bfx) {
+    *bx = C::RX;
+    *by = C::RY;
+    *bfx = C::RXF;
 }
 
 }  // namespace
 
-int jacobi_max_sweeps_per_launch() { return Cfg::HALO < RtA::HALO ? Cfg::HALO : RtA::HALO; }
+int jacobi_max_sweeps_per_launch() { return Tb::HALO < RtA::HALO ? Tb::HALO : RtA::HALO; }
 
 int jacobi_config(Grid g) {
-    if (variant() == 0) return 0;
-    return rt_cost<RtB>(g) < rt_cost<RtA>(g) ? 2 : 1;
+    if (force_tb()) return JACOBI_TB;
+    // grids narrower than one register tile waste most of its 128 columns
+    if (g.W <= 96) return JACOBI_TB;
+    return rt_cost<RtB>(g) < rt_cost<RtA>(g) ? JACOBI_RT_B : JACOBI_RT_A;
 }
 
-bool jacobi_encode_maps(JacobiMaps* maps, float* p0, float* p1, float* div, uint8_t* flags,
-                        Grid g, const char** err) {
-    const int cfg = jacobi_config(g);
-    int bx = Cfg::RX, by = Cfg::RY, bfx = Cfg::RXF;
-    if (cfg == 1) bx = RtA::RX, by = RtA::RY, bfx = RtA::RXF;
-    if (cfg == 2) bx = RtB::RX, by = RtB::RY, bfx = RtB::RXF;
-    maps->config = cfg;
+void jacobi_tile(int config, int* tx, int* ty) {
+    switch (config) {
+        case JACOBI_RT_A: *tx = RtA::TX; *ty = RtA::TY; break;
+        case JACOBI_RT_B: *tx = RtB::TX; *ty = RtB::TY; break;
+        default: *tx = Tb::TX; *ty = Tb::TY; break;
+    }
+}
+
+bool jacobi_encode_maps_for(JacobiMaps* maps, int config, float* p0, float* p1, float* div,
+                            uint8_t* flags, Grid g, const char** err) {
+    int bx, by, bfx;
+    if (config == JACOBI_RT_A)
+        box_of<RtA>(&bx, &by, &bfx);
+    else if (config == JACOBI_RT_B)
+        box_of<RtB>(&bx, &by, &bfx);
+    else
+        box_of<Tb>(&bx, &by, &bfx);
+    maps->config = config;
     return encode_2d(&maps->p[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p0, g, bx, by, err) &&
            encode_2d(&maps->p[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p1, g, bx, by, err) &&
            encode_2d(&maps->div, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, div, g, bx, by, err) &&
            encode_2d(&maps->flags, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, flags, g, bfx, by, err);
 }
 
-cudaError_t launch_jacobi(const JacobiMaps& maps, float* const pbuf[2], int src, Grid g,
-                          int sweeps, int* status, cudaStream_t st) {
+cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbuf[2], int src,
+                          Grid g, int sweeps, int* status, cudaStream_t st) {
     if (sweeps < 1 || sweeps > jacobi_max_sweeps_per_launch()) return cudaErrorInvalidValue;
-    if (maps.config == 1) return launch_rt<RtA>(maps, pbuf, src, g, sweeps, status, st);
-    if (maps.config == 2) return launch_rt<RtB>(maps, pbuf, src, g, sweeps, status, st);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_jacobi_tb,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
-    dim3 grid((g.W + Cfg::TX - 1) / Cfg::TX, (g.H + Cfg::TY - 1) / Cfg::TY);
-    dim3 block(Cfg::THREADS_X, Cfg::THREADS_Y);
-    k_jacobi_tb<<<grid, block, Cfg::SMEM, st>>>(maps.p[src], maps.div, maps.flags,
-                                                pbuf[1 - src], g, sweeps, status);
-    return cudaGetLastError();
+    int tx, ty;
+    jacobi_tile(config, &tx, &ty);
+    const int tiles_x = (g.W + tx - 1) / tx, tiles_y = (g.H + ty - 1) / ty;
+    const GridJobs jobs{&d_maps->p[src], &d_maps->div, &d_maps->flags, pbuf[1 - src], g,
+                        sweeps, tiles_x, tiles_x * tiles_y, tx, ty};
+    if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st);
+    if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st);
+    return launch_tb_jobs<Tb>(jobs, status, st);
+}
+
+cudaError_t launch_jacobi_batch(int config, const JacobiBatchItem* items, int n_items,
+                                const JacobiBatchSim* sims, int* status, cudaStream_t st) {
+    const BatchJobs jobs{items, sims, n_items};
+    if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st);
+    if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st);
+    return launch_tb_jobs<Tb>(jobs, status, st);
 }
 
 }  // namespace natrix

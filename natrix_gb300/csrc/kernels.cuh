@@ -111,25 +111,47 @@ cudaError_t launch_residual(const float* p, const float* div, const uint8_t* mas
                             double* partials, double* out, cudaStream_t st);
 
 // ---- Jacobi (jacobi_tma.cu) ------------------------------------------------
-// Tensor maps of one solver grid for the temporally blocked sweep kernel.
+// Jacobi tile kernels: shared-memory sweeps on 64x32 tiles, or register tiled
+// with 112x112 / 112x128 output tiles.
+enum JacobiConfig : int { JACOBI_TB = 0, JACOBI_RT_A = 1, JACOBI_RT_B = 2 };
+
+// Tensor maps of one grid for the sweep kernels, encoded for one
+// configuration's boxes.  Kernels read them from device memory (64-byte
+// aligned: cudaMalloc'd).
 struct JacobiMaps {
     CUtensorMap p[2];  // pressure ping-pong buffers as sources
     CUtensorMap div;
     CUtensorMap flags;
-    int config;  // kernel configuration the boxes were encoded for
+    int config;
 };
 
-// Kernel configuration picked for a grid (0 = shared-memory sweeps,
-// 1 / 2 = register-tiled persistent with 112x112 / 112x128 output tiles).
-int jacobi_config(Grid g);
+// One simulation of a batch, as the batched sweep kernels see it.
+struct JacobiBatchSim {
+    JacobiMaps maps;
+    float* p[2];
+    Grid g;
+};
+
+// One tile of one batched launch.
+struct JacobiBatchItem {
+    int sim, src, sweeps, tile_x, tile_y;
+};
 
 // Largest sweep count one launch fuses (the tile halo).
 int jacobi_max_sweeps_per_launch();
-// Encode the tensor maps for the buffers (returns false + message on error).
-bool jacobi_encode_maps(JacobiMaps* maps, float* p0, float* p1, float* div, uint8_t* flags,
-                        Grid g, const char** err);
-// `sweeps` (1..max) Jacobi sweeps from p[src] into p[1 - src].
-cudaError_t launch_jacobi(const JacobiMaps& maps, float* const pbuf[2], int src, Grid g,
-                          int sweeps, int* status, cudaStream_t st);
+// Configuration chosen for a single grid (tile shape against SM count).
+int jacobi_config(Grid g);
+// Output tile of a configuration.
+void jacobi_tile(int config, int* tx, int* ty);
+// Encode the tensor maps of the buffers for a configuration (false + message on error).
+bool jacobi_encode_maps_for(JacobiMaps* maps, int config, float* p0, float* p1, float* div,
+                            uint8_t* flags, Grid g, const char** err);
+// `sweeps` (1..max) Jacobi sweeps of one grid from pbuf[src] into pbuf[1 - src];
+// `d_maps` is the device copy of the grid's maps.
+cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbuf[2], int src,
+                          Grid g, int sweeps, int* status, cudaStream_t st);
+// One batched launch: every item is one tile of one simulation (device arrays).
+cudaError_t launch_jacobi_batch(int config, const JacobiBatchItem* items, int n_items,
+                                const JacobiBatchSim* sims, int* status, cudaStream_t st);
 
 }  // namespace natrix

@@ -5,407 +5,61 @@
 // One thread per cell, 32x8 blocks (a warp spans 32 consecutive cells of a
 // row, so float2 velocity loads and stores coalesce into 256-byte segments).
 // Compiled with -fmad=false: see common.cuh for the arithmetic contract.
-#include "kernels.cuh"
+#include "cells.cuh"
 
 namespace natrix {
 
 namespace {
 
-constexpr int BX = 32, BY = 8;
-
 inline dim3 grid_for(const Grid& g) { return dim3((g.W + BX - 1) / BX, (g.H + BY - 1) / BY); }
-
-// ---------------------------------------------------------------- obstacles
-// shader.AddCircleObstacle.comp:17-37 and shader.AddTriangleObstacle.comp:19-52,
-// all queued shapes in one pass; `fresh` = start from an empty mask (the
-// reference clears the obstacle buffer at the end of every update).
-__device__ __forceinline__ float tri_sign(float p1x, float p1y, float p2x, float p2y,
-                                          float p3x, float p3y) {
-    return ((p1x - p3x) * (p2y - p3y)) - ((p2x - p3x) * (p1y - p3y));
-}
-
-// Block-level culling: warp 0 compacts, in order, the indices of the ops
-// whose conservative footprint (expanded by one cell) meets this block's
-// cells; `test(k)` decides.  Every cell then walks the kept list only.
-template <class Test>
-__device__ __forceinline__ int cull_ops(int n, int* kept, Test test) {
-    __shared__ int s_n;
-    if (threadIdx.y == 0) {
-        int count = 0;
-        for (int base = 0; base < n; base += 32) {
-            const int k = base + threadIdx.x;
-            const bool keep = k < n && test(k);
-            const unsigned m = __ballot_sync(0xffffffffu, keep);
-            if (keep) kept[count + __popc(m & ((1u << threadIdx.x) - 1u))] = k;
-            count += __popc(m);
-        }
-        if (threadIdx.x == 0) s_n = count;
-    }
-    __syncthreads();
-    return s_n;
-}
-
-// Does a disc of radius `r` around (cx, cy) meet the cell box [x0,x1]x[y0,y1]?
-// (conservative: one cell of margin)
-__device__ __forceinline__ bool disc_meets_box(float cx, float cy, float r, int x0, int x1,
-                                               int y0, int y1) {
-    const float dx = fmaxf(fmaxf((float)x0 - cx, cx - (float)x1), 0.0f);
-    const float dy = fmaxf(fmaxf((float)y0 - cy, cy - (float)y1), 0.0f);
-    const float rr = r + 1.0f;
-    return dx * dx + dy * dy <= rr * rr;
-}
 
 __global__ void __launch_bounds__(BX* BY)
     k_obstacles(uint8_t* __restrict__ mask, Grid g, const ShapeOp* __restrict__ ops, int n,
                 int fresh) {
-    __shared__ ShapeOp s_ops[kMaxOpsPerLaunch];
-    __shared__ int s_kept[kMaxOpsPerLaunch];
-    const int tid = threadIdx.y * BX + threadIdx.x;
-    for (int i = tid; i < n; i += BX * BY) s_ops[i] = ops[i];
-    __syncthreads();
-    const int bx0 = blockIdx.x * BX, by0 = blockIdx.y * BY;
-    const int bx1 = bx0 + BX - 1, by1 = by0 + BY - 1;
-    const int nk = cull_ops(n, s_kept, [&](int k) {
-        const ShapeOp& op = s_ops[k];
-        // triangles are never culled: the reference's same-sign test marks
-        // cells far outside a degenerate (zero-area) triangle's bounding box
-        if (op.kind != SHAPE_CIRCLE) return true;
-        return disc_meets_box(op.a[0] * (float)g.W, op.a[1] * (float)g.H, op.a[2], bx0, bx1,
-                              by0, by1);
-    });
-    const int x = bx0 + threadIdx.x, y = by0 + threadIdx.y;
-    if (x >= g.W || y >= g.H) return;
-    const size_t i = (size_t)y * g.P + x;
-    if (nk == 0 && !fresh) return;
-    uint8_t m = fresh ? 0 : mask[i];
-    for (int kk = 0; kk < nk; ++kk) {
-        const ShapeOp& op = s_ops[s_kept[kk]];
-        if (op.kind == SHAPE_CIRCLE) {
-            const float spx = op.a[0] * (float)g.W, spy = op.a[1] * (float)g.H;
-            const float dx = spx - (float)x, dy = spy - (float)y;
-            if (sqrtf(dx * dx + dy * dy) <= op.a[2]) m = 1;  // vec2(1, 0), both branches
-        } else {
-            const float ptx = (float)x / (float)g.W, pty = (float)y / (float)g.H;
-            const bool b1 = tri_sign(ptx, pty, op.a[0], op.a[1], op.a[2], op.a[3]) < 0.0f;
-            const bool b2 = tri_sign(ptx, pty, op.a[2], op.a[3], op.a[4], op.a[5]) < 0.0f;
-            const bool b3 = tri_sign(ptx, pty, op.a[4], op.a[5], op.a[0], op.a[1]) < 0.0f;
-            if (b1 == b2 && b2 == b3) m = (uint8_t)((m & ~3) | (op.is_static ? 2 : 1));
-        }
-    }
-    mask[i] = m;
-}
-
-// ------------------------------------------------------------------ forcing
-// Queued forcing ops applied in order to each cell of the velocity grid
-// and/or the density grid (both when they have the same size).
-//  FORCE_CONE_VELOCITY  shader.AddVelocity.comp:26-35: inside the radius
-//      v += V*(r - d)/r, then every cell is clamped to [-1, 1].
-//  FORCE_GAUSS          w = exp(-d^2/r^2) inside 3r: v = clamp(v + w V, -1, 1)
-//      for every cell, rho = clamp(rho + w s, 0, 255) inside the cut-off.
-//  FORCE_CONE_DENSITY   demo/shaders/shader.AddParticle.comp:25-34 on rows the
-//      reference's dispatch reaches.
-// Ops whose footprint misses the block are culled.  For velocity that is
-// exact because a velocity op outside its footprint is a clamp, and clamp is
-// idempotent: the only trace a culled or missing op leaves is the clamp of the
-// first velocity op when it does not touch the cell (a cell whose first op
-// touches it starts from the unclamped value, as in the reference).
-__device__ __forceinline__ bool op_is_velocity(int kind) {
-    return kind == FORCE_CONE_VELOCITY || kind == FORCE_GAUSS;
+    block_obstacles(mask, g, ops, n, fresh, blockIdx.x * BX, blockIdx.y * BY);
 }
 
 __global__ void __launch_bounds__(BX* BY)
     k_forcing(float2* __restrict__ vel, Grid gv, float* __restrict__ rho, Grid gd,
               const ForceOp* __restrict__ ops, int n) {
-    __shared__ ForceOp s_ops[kMaxOpsPerLaunch];
-    __shared__ int s_kept[kMaxOpsPerLaunch];
-    const int tid = threadIdx.y * BX + threadIdx.x;
-    for (int i = tid; i < n; i += BX * BY) s_ops[i] = ops[i];
-    __syncthreads();
-    const int bx0 = blockIdx.x * BX, by0 = blockIdx.y * BY;
-    const int bx1 = bx0 + BX - 1, by1 = by0 + BY - 1;
-    const int x = bx0 + threadIdx.x, y = by0 + threadIdx.y;
-    if (vel) {
-        int first_vel = -1;
-        for (int k = 0; k < n; ++k)
-            if (op_is_velocity(s_ops[k].kind)) {
-                first_vel = k;
-                break;
-            }
-        const int nk = cull_ops(n, s_kept, [&](int k) {
-            const ForceOp& op = s_ops[k];
-            if (op.kind == FORCE_CONE_VELOCITY)
-                return disc_meets_box(op.px * (float)gv.W, op.py * (float)gv.H, op.r, bx0, bx1,
-                                      by0, by1);
-            if (op.kind == FORCE_GAUSS)
-                return disc_meets_box(op.px * (float)gv.W, op.py * (float)gv.H, 3.0f * op.r, bx0,
-                                      bx1, by0, by1);
-            return false;
-        });
-        if (first_vel >= 0 && x < gv.W && y < gv.H) {
-            const size_t i = (size_t)y * gv.P + x;
-            float2 a = vel[i];
-            // the first velocity op culled for this block: it clamps the cell
-            bool started = !(nk > 0 && s_kept[0] == first_vel);
-            if (started) {
-                a.x = clampf(a.x, -1.0f, 1.0f);
-                a.y = clampf(a.y, -1.0f, 1.0f);
-            }
-            for (int kk = 0; kk < nk; ++kk) {
-                const ForceOp& op = s_ops[s_kept[kk]];
-                bool hit = false;
-                float ax = a.x, ay = a.y;
-                if (op.kind == FORCE_CONE_VELOCITY) {
-                    const float spx = op.px * (float)gv.W, spy = op.py * (float)gv.H;
-                    const float dx = spx - (float)x, dy = spy - (float)y;
-                    const float len = sqrtf(dx * dx + dy * dy);
-                    if (len <= op.r) {
-                        ax = a.x + op.vx * (op.r - len) / op.r;
-                        ay = a.y + op.vy * (op.r - len) / op.r;
-                        hit = true;
-                    }
-                } else {
-                    const float cx = op.px * (float)gv.W, cy = op.py * (float)gv.H;
-                    const float dx = (float)x - cx, dy = (float)y - cy;
-                    const float cut = 3.0f * op.r;
-                    if (dx * dx + dy * dy <= cut * cut) {
-                        const float w = nx_expf(-(dx * dx + dy * dy) / (op.r * op.r));
-                        ax = a.x + w * op.vx;
-                        ay = a.y + w * op.vy;
-                        hit = true;
-                    }
-                }
-                if (hit || !started) {
-                    a.x = clampf(ax, -1.0f, 1.0f);
-                    a.y = clampf(ay, -1.0f, 1.0f);
-                    started = true;
-                }
-            }
-            vel[i] = a;
-        }
-        __syncthreads();  // s_kept is reused below
-    }
-    if (rho) {
-        const int nk = cull_ops(n, s_kept, [&](int k) {
-            const ForceOp& op = s_ops[k];
-            if (op.kind == FORCE_GAUSS)
-                return disc_meets_box(op.px * (float)gd.W, op.py * (float)gd.H, 3.0f * op.r, bx0,
-                                      bx1, by0, by1);
-            if (op.kind == FORCE_CONE_DENSITY)
-                return by0 < op.rows && disc_meets_box(op.px * (float)gd.W, op.py * (float)gd.H,
-                                                       op.r, bx0, bx1, by0, by1);
-            return false;
-        });
-        if (nk > 0 && x < gd.W && y < gd.H) {
-            const size_t i = (size_t)y * gd.P + x;
-            float a = rho[i];
-            for (int kk = 0; kk < nk; ++kk) {
-                const ForceOp& op = s_ops[s_kept[kk]];
-                if (op.kind == FORCE_GAUSS) {
-                    const float cx = op.px * (float)gd.W, cy = op.py * (float)gd.H;
-                    const float dx = (float)x - cx, dy = (float)y - cy;
-                    const float cut = 3.0f * op.r;
-                    if (dx * dx + dy * dy <= cut * cut) {
-                        const float w = nx_expf(-(dx * dx + dy * dy) / (op.r * op.r));
-                        a = clampf(a + w * op.s, 0.0f, 255.0f);
-                    }
-                } else if (y < op.rows) {
-                    const float spx = op.px * (float)gd.W, spy = op.py * (float)gd.H;
-                    const float dx = spx - (float)x, dy = spy - (float)y;
-                    const float len = sqrtf(dx * dx + dy * dy);
-                    if (len <= op.r) a = clampf(a + op.s * (op.r - len) / op.r, 0.0f, 255.0f);
-                }
-            }
-            rho[i] = a;
-        }
-    }
+    block_forcing(vel, gv, rho, gd, ops, n, blockIdx.x * BX, blockIdx.y * BY);
 }
 
-// ---------------------------------------------------------------- advection
-// shader.AdvectVelocity.comp:19-51, with shader.InitBoundaries.comp:11-35
-// fused: the reference zeroes the border of the read buffer in place before
-// advecting, so border cells read as zero here (centre and gathers alike).
-__device__ __forceinline__ float2 vel_at(const float2* __restrict__ v, const Grid& g, int x,
-                                         int y, bool zero_border) {
-    if (zero_border && (x == 0 || x == g.W - 1 || y == 0 || y == g.H - 1))
-        return make_float2(0.0f, 0.0f);
-    return __ldg(v + (size_t)y * g.P + x);
-}
-
-__global__ void __launch_bounds__(BX* BY)
-    k_advect(const float2* __restrict__ vin, float2* __restrict__ vout,
+__global__ void __launch_bounds__(BX* BY) k_advect(const float2* __restrict__ vin, float2* __restrict__ vout,
              const uint8_t* __restrict__ mask, Grid g, const StepParams* __restrict__ sp) {
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-    if (x >= g.W || y >= g.H) return;
-    const size_t i = (size_t)y * g.P + x;
-    const bool zb = sp->has_borders != 0;
-    if (!sp->mask_zero && mask[i]) {
-        vout[i] = make_float2(0.0f, 0.0f);
-        return;
-    }
-    const float dt = sp->dt, speed = sp->speed, diss = sp->dissipation;
-    const float2 vel = vel_at(vin, g, x, y, zb);
-    const float fx = (float)x - vel.x * dt * speed;
-    const float fy = (float)y - vel.y * dt * speed;
-    const Corners c = corners(fx, fy, g.W, g.H);
-    const float2 lt = vel_at(vin, g, c.lo_x, c.hi_y, zb);
-    const float2 rt = vel_at(vin, g, c.hi_x, c.hi_y, zb);
-    const float2 lb = vel_at(vin, g, c.lo_x, c.lo_y, zb);
-    const float2 rb = vel_at(vin, g, c.hi_x, c.lo_y, zb);
-    const float h1x = mixf(lt.x, rt.x, c.dx), h1y = mixf(lt.y, rt.y, c.dx);
-    const float h2x = mixf(lb.x, rb.x, c.dx), h2y = mixf(lb.y, rb.y, c.dx);
-    const float sx = mixf(h2x, h1x, c.dy), sy = mixf(h2y, h1y, c.dy);
-    vout[i] = make_float2(clampf(sx * diss, -1.0f, 1.0f), clampf(sy * diss, -1.0f, 1.0f));
+    cell_advect(vin, vout, mask, g, sp, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
 }
 
-// Clamped neighbour coordinates (natrix/core/shaders/originals/common.sh:9-19).
-struct Nbr {
-    size_t c, l, r, b, t;
-};
-__device__ __forceinline__ Nbr nbrs(const Grid& g, int x, int y) {
-    Nbr n;
-    const int xl = x > 0 ? x - 1 : 0, xr = x < g.W - 1 ? x + 1 : g.W - 1;
-    const int yb = y > 0 ? y - 1 : 0, yt = y < g.H - 1 ? y + 1 : g.H - 1;
-    n.c = (size_t)y * g.P + x;
-    n.l = (size_t)y * g.P + xl;
-    n.r = (size_t)y * g.P + xr;
-    n.b = (size_t)yb * g.P + x;
-    n.t = (size_t)yt * g.P + x;
-    return n;
+__global__ void __launch_bounds__(BX* BY) k_calc_vorticity(const float2* __restrict__ v, float* __restrict__ w, Grid g) {
+    cell_calc_vorticity(v, w, g, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
 }
 
-// ------------------------------------------------------ vorticity confinement
-// shader.CalcVorticity.comp:13-27.
-__global__ void __launch_bounds__(BX* BY)
-    k_calc_vorticity(const float2* __restrict__ v, float* __restrict__ w, Grid g) {
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-    if (x >= g.W || y >= g.H) return;
-    const Nbr n = nbrs(g, x, y);
-    const float2 vl = __ldg(v + n.l), vr = __ldg(v + n.r), vb = __ldg(v + n.b),
-                 vt = __ldg(v + n.t);
-    w[n.c] = 0.5f * ((vr.y - vl.y) - (vt.x - vb.x));
-}
-
-// shader.ApplyVorticity.comp:19-40.
-__global__ void __launch_bounds__(BX* BY)
-    k_apply_vorticity(const float2* __restrict__ vin, float2* __restrict__ vout,
+__global__ void __launch_bounds__(BX* BY) k_apply_vorticity(const float2* __restrict__ vin, float2* __restrict__ vout,
                       const float* __restrict__ w, Grid g, const StepParams* __restrict__ sp) {
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-    if (x >= g.W || y >= g.H) return;
-    const Nbr n = nbrs(g, x, y);
-    const float wl = __ldg(w + n.l), wr = __ldg(w + n.r), wb = __ldg(w + n.b),
-                wt = __ldg(w + n.t), wc = __ldg(w + n.c);
-    float fx = 0.5f * (fabsf(wt) - fabsf(wb));
-    float fy = 0.5f * (fabsf(wr) - fabsf(wl));
-    const float eps = 2.4414e-4f;
-    const float d = fx * fx + fy * fy;
-    const float m = eps > d ? eps : d;
-    const float rs = 1.0f / sqrtf(m);  // inversesqrt, correctly rounded
-    fx = fx * rs;
-    fy = fy * rs;
-    const float s = sp->vorticity * wc;
-    fx = fx * (s * 1.0f);
-    fy = fy * (s * -1.0f);
-    const float dt = sp->dt;
-    const float2 v = vin[n.c];
-    vout[n.c] = make_float2(v.x + fx * dt, v.y + fy * dt);
+    cell_apply_vorticity(vin, vout, w, g, sp, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
 }
 
-// ---------------------------------------------------------------- viscosity
-// shader.Viscosity.comp:17-32, one smoothing sweep.
-__global__ void __launch_bounds__(BX* BY)
-    k_viscosity(const float2* __restrict__ vin, float2* __restrict__ vout, Grid g,
+__global__ void __launch_bounds__(BX* BY) k_viscosity(const float2* __restrict__ vin, float2* __restrict__ vout, Grid g,
                 const StepParams* __restrict__ sp) {
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-    if (x >= g.W || y >= g.H) return;
-    const Nbr n = nbrs(g, x, y);
-    const float alpha = sp->alpha, rbeta = sp->rbeta;
-    const float2 a = __ldg(vin + n.l), b = __ldg(vin + n.r), c = __ldg(vin + n.b),
-                 d = __ldg(vin + n.t), e = __ldg(vin + n.c);
-    vout[n.c] = make_float2((a.x + b.x + c.x + d.x + e.x * alpha) * rbeta,
-                            (a.y + b.y + c.y + d.y + e.y * alpha) * rbeta);
+    cell_viscosity(vin, vout, g, sp, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
 }
 
-// --------------------------------------------------------------- divergence
-// shader.Divergence.comp:15-41.  Also writes, for the pressure sweeps, the
-// neighbour-substitution flags and the first Jacobi sweep from the zero guess:
-// with p = 0 everywhere, shader.Poisson.comp:37 gives (0+0+0+0 - b)*0.25,
-// which is (0 - b)*0.25 bit for bit; the reference's clear of the pressure
-// buffer (fluid_simulator.py:235-248) is thereby folded away.
-__global__ void __launch_bounds__(BX* BY)
-    k_divergence(const float2* __restrict__ v, const uint8_t* __restrict__ mask,
+__global__ void __launch_bounds__(BX* BY) k_divergence(const float2* __restrict__ v, const uint8_t* __restrict__ mask,
                  float* __restrict__ div, uint8_t* __restrict__ flags, float* __restrict__ p1,
                  Grid g, const StepParams* __restrict__ sp) {
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-    if (x >= g.W || y >= g.H) return;
-    const Nbr n = nbrs(g, x, y);
-    const bool mz = sp->mask_zero != 0;
-    const bool ol = !mz && mask[n.l], orr = !mz && mask[n.r];
-    const bool ob = !mz && mask[n.b], ot = !mz && mask[n.t];
-    const float x1 = ol ? 0.0f : __ldg(v + n.l).x;
-    const float x2 = orr ? 0.0f : __ldg(v + n.r).x;
-    const float y1 = ob ? 0.0f : __ldg(v + n.b).y;
-    const float y2 = ot ? 0.0f : __ldg(v + n.t).y;
-    const float b = 0.5f * ((x2 - x1) + (y2 - y1));
-    div[n.c] = b;
-    uint8_t f = 0;
-    if (x == 0 || ol) f |= NB_L;
-    if (x == g.W - 1 || orr) f |= NB_R;
-    if (y == 0 || ob) f |= NB_B;
-    if (y == g.H - 1 || ot) f |= NB_T;
-    flags[n.c] = f;
-    if (p1) p1[n.c] = (0.0f - b) * 0.25f;
+    cell_divergence(v, mask, div, flags, p1, g, sp, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
 }
 
-// -------------------------------------------------------- gradient subtract
-// shader.SubtractGradient.comp:17-47 (same neighbour rule as the sweep).
-__global__ void __launch_bounds__(BX* BY)
-    k_subtract_gradient(const float2* __restrict__ vin, float2* __restrict__ vout,
+__global__ void __launch_bounds__(BX* BY) k_subtract_gradient(const float2* __restrict__ vin, float2* __restrict__ vout,
                         const float* __restrict__ p, const uint8_t* __restrict__ flags,
                         Grid g) {
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-    if (x >= g.W || y >= g.H) return;
-    const Nbr n = nbrs(g, x, y);
-    const uint8_t f = flags[n.c];
-    const float pc = __ldg(p + n.c);
-    const float x1 = (f & NB_L) ? pc : __ldg(p + n.l);
-    const float x2 = (f & NB_R) ? pc : __ldg(p + n.r);
-    const float y1 = (f & NB_B) ? pc : __ldg(p + n.b);
-    const float y2 = (f & NB_T) ? pc : __ldg(p + n.t);
-    float2 vel = vin[n.c];
-    vel.x -= 0.5f * (x2 - x1);
-    vel.y -= 0.5f * (y2 - y1);
-    vout[n.c] = vel;
+    cell_subtract_gradient(vin, vout, p, flags, g, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
 }
 
-// --------------------------------------------------------- density advection
-// demo/shaders/shader.AdvectParticle.comp:21-71: the density grid (its own
-// size) is advected by the velocity sampled at the matching position of the
-// velocity grid, scaled by the grid-size ratio.
-__global__ void __launch_bounds__(BX* BY)
-    k_density_advect(const float* __restrict__ rin, float* __restrict__ rout, Grid gd,
+__global__ void __launch_bounds__(BX* BY) k_density_advect(const float* __restrict__ rin, float* __restrict__ rout, Grid gd,
                      const float2* __restrict__ v, const uint8_t* __restrict__ mask, Grid gv,
                      const StepParams* __restrict__ sp) {
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-    if (x >= gd.W || y >= gd.H) return;
-    const size_t i = (size_t)y * gd.P + x;
-    const float nx = (float)x / (float)gd.W * (float)gv.W;
-    const float ny = (float)y / (float)gd.H * (float)gv.H;
-    if (!sp->mask_zero) {
-        const size_t oi = (size_t)(unsigned)ny * gv.P + (unsigned)nx;
-        if (mask[oi]) {
-            rout[i] = 0.0f;
-            return;
-        }
-    }
-    const Corners cv = corners(nx, ny, gv.W, gv.H);
-    float2 u = sample_vel(v, gv.P, cv);
-    u.x = u.x * ((float)gd.W / (float)gv.W);
-    u.y = u.y * ((float)gd.H / (float)gv.H);
-    const float dt = sp->dt, speed = sp->d_speed;
-    const float fx = (float)x - u.x * dt * speed;
-    const float fy = (float)y - u.y * dt * speed;
-    const Corners c = corners(fx, fy, gd.W, gd.H);
-    rout[i] = sample_scalar(rin, gd.P, c) * sp->d_dissipation;
+    cell_density_advect(rin, rout, gd, v, mask, gv, sp, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
 }
 
 // ----------------------------------------------------------------- residual

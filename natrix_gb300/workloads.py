@@ -67,6 +67,39 @@ def uniform_particles(seed: int, n: int, width: int, height: int) -> np.ndarray:
     return np.ascontiguousarray(pos[np.argsort(key, kind="stable")])
 
 
+@dataclass(frozen=True)
+class BatchWorkload:
+    """Many independent simulations: side lengths log-uniform in [64, 512]
+    rounded to multiples of 16, Jacobi counts uniform in {20, 40, 80}, 0-6
+    discs each, 8 Gaussian splats per simulation per step, eps 0, nu 0."""
+
+    name: str
+    n_sims: int
+    steps: int
+    splats_per_step: int = 8
+    seed: int = 0
+
+    def sides(self) -> np.ndarray:
+        rng = np.random.default_rng([self.seed, 4])
+        s = np.exp(rng.uniform(np.log(64), np.log(512), self.n_sims))
+        return (16 * np.round(s / 16)).astype(np.int32)
+
+    def iterations(self) -> np.ndarray:
+        rng = np.random.default_rng([self.seed, 5])
+        return rng.choice(np.array([20, 40, 80]), self.n_sims)
+
+    def obstacles(self, sim: int, side: int) -> np.ndarray:
+        rng = np.random.default_rng([self.seed, 6, sim])
+        return circle_obstacles(rng, int(rng.integers(0, 7)), side, side)
+
+    def forcing(self, sim: int, step: int, side: int) -> np.ndarray:
+        rng = np.random.default_rng([self.seed, 7, sim, step])
+        return gauss_splats(rng, self.splats_per_step, side, side, 5.0)
+
+
+BATCH_512 = BatchWorkload("batch-512-sims-64to512-K20/40/80", 512, 100)
+
+
 def gauss_splats(rng: np.random.Generator, n: int, width: int, height: int,
                  speed: float, radius_frac: float = 0.02,
                  amp_cells_per_s: float = 5.0) -> np.ndarray:
