@@ -30,6 +30,8 @@ UNITS = {
     "noalloc.cu": ["-fmad=false"],
     "particles.cu": ["-fmad=false"],
     "batch.cu": ["-fmad=false"],
+    "unet_conv.cu": [],
+    "unet_kernels.cu": [],
 }
 
 

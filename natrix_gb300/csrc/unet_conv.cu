@@ -1,0 +1,361 @@
+// 3x3 convolutions (stride 1, zero padding 1) of NHWC bf16 activations as
+// implicit GEMMs on the 5th-generation tensor cores: BF16 operands, FP32
+// accumulation in TMEM.  Used by the U-Net warm start for the forward pass
+// and, with flipped and transposed weights, for the input gradient.
+//
+// GEMM view: D[pixel, n] = sum over taps t and input channels c of
+//     X[pixel + offset(t), c] * Wp[n, t, c]
+// M = 128 pixels of one image row, N = output channels, K = 9 * C.
+//
+// One persistent CTA per SM, six warps:
+//   warp 0 lane 0  TMA producer: per tap, one 4-D box {8 channels, 128 px}
+//                  per 8-channel chunk (out-of-image pixels and channels read
+//                  as zero, which is the padding), into a 4-stage ring;
+//   warp 1 lane 0  MMA issuer: per tap, C/16 tcgen05.mma (K = 16 each) into
+//                  one of two TMEM accumulators; tcgen05.commit releases the
+//                  ring stage and, after the last tap, hands the accumulator
+//                  to the epilogue;
+//   warps 2-5      epilogue: tcgen05.ld of their 32-lane quarter, bias, ReLU
+//                  or ReLU-gate, optional 1x1 head, bf16 NHWC stores.
+// The weights (packed once per layer in the operand layout) are copied to
+// shared memory once per CTA with cp.async.bulk.
+//
+// Operand layout (validated SWIZZLE_NONE K-major, see umma.cuh): a TMA box of
+// 8 channels x 128 pixels lands as 16 consecutive 8x16-byte core matrices,
+// so chunk q of a stage starts at q * 2048 bytes: LBO = 2048, SBO = 128.  The
+// packed weights use LBO = N/8 * 128, SBO = 128 with K chunks ordered
+// (tap, channel chunk).
+//
+// Every wait is bounded; a role that gives up records status bit 2 and
+// leaves its loop, the others then time out too, and the allocating warp
+// frees TMEM before the CTA exits.
+#include <cudaTypedefs.h>
+
+#include <cstdio>
+
+#include "../../include/natrix.h"
+#include "../../include/natrix_nn.h"
+#include "kernels.cuh"
+#include "umma.cuh"
+
+namespace natrix {
+
+namespace {
+
+constexpr int kStages = 4;
+constexpr int kTileM = 128;
+constexpr int kChunkBytes = 8 * kTileM * 2;  // one 8-channel box: 2048 B
+
+struct ConvParams {
+    int B, H, W;
+    int c0, c1;      // channels of source 0 / source 1 (multiples of 8; c1 may be 0)
+    int ctot;        // c0 + c1 rounded up to a multiple of 16 (zero chunks read as padding)
+    int N;           // output channels (multiple of 16, <= 128)
+    const uint16_t* wpack;  // packed bf16 weights, N x 9*ctot, operand layout
+    const float* bias;      // N or null
+    int relu;               // 1: ReLU on the output
+    const uint16_t* gate;   // NHWC bf16 with `N` channels or null: out *= (gate > 0)
+    uint16_t* out0;         // NHWC bf16, channels [0, n0), or null
+    int n0;
+    uint16_t* out1;         // NHWC bf16, channels [n0, N), or null
+    const float* head_w;    // N weights of a 1x1 head, or null
+    float head_b;
+    float* head_out;        // B*H*W floats, or null
+    int* status;
+    int tiles_x, n_tiles;
+    uint32_t smem_w, smem_a;  // byte offsets in dynamic shared memory
+    uint32_t tmem_cols;
+};
+
+__device__ __forceinline__ float bf16_to_f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
+
+__device__ __forceinline__ uint16_t f_to_bf16(float f) {
+    // round to nearest even
+    uint32_t u = __float_as_uint(f);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+__global__ void __launch_bounds__(192, 1)
+    k_conv3x3_tc(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
+                 const ConvParams P) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2], wbar;
+    __shared__ uint32_t tmem_slot;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chunks = P.ctot / 8;  // 8-channel chunks per tap
+    const int c0_chunks = P.c0 / 8;
+    const int c1_chunks = P.c1 / 8;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            umma::mbar_init(&full[s], 1);
+            umma::mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            umma::mbar_init(&acc_full[a], 1);
+            umma::mbar_init(&acc_empty[a], 4);
+        }
+        umma::mbar_init(&wbar, 1);
+        umma::mbar_init_fence();
+    }
+    if (warp == 1) umma::tmem_alloc(&tmem_slot, P.tmem_cols);
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t wbytes = (uint32_t)P.N * 9u * (uint32_t)P.ctot * 2u;
+
+    if (warp == 0 && lane == 0) {
+        // weights once, then the activation ring
+        umma::mbar_arrive_expect_tx(&wbar, wbytes);
+        for (uint32_t off = 0; off < wbytes; off += 32768u) {
+            const uint32_t n = wbytes - off < 32768u ? wbytes - off : 32768u;
+            umma::bulk_load(smem + P.smem_w + off, reinterpret_cast<const unsigned char*>(P.wpack) + off,
+                            n, &wbar);
+        }
+        int s = 0;
+        uint32_t phase = 0;
+        bool ok = true;
+        for (int tile = blockIdx.x; tile < P.n_tiles && ok; tile += gridDim.x) {
+            const int tx = tile % P.tiles_x, rest = tile / P.tiles_x;
+            const int y = rest % P.H, b = rest / P.H;
+            const int x0 = tx * kTileM;
+            for (int t = 0; t < 9 && ok; ++t) {
+                const int dy = t / 3 - 1, dx = t % 3 - 1;
+                if (!umma::mbar_wait(&empty[s], phase ^ 1u)) {
+                    ok = false;
+                    break;
+                }
+                umma::mbar_arrive_expect_tx(&full[s], (uint32_t)chunks * kChunkBytes);
+                unsigned char* dst = smem + P.smem_a + (uint32_t)s * chunks * kChunkBytes;
+                for (int q = 0; q < chunks; ++q) {
+                    if (q < c0_chunks || c1_chunks == 0)
+                        umma::tma_load_4d(dst + q * kChunkBytes, &tm0, 8 * q, x0 + dx, y + dy, b,
+                                          &full[s]);
+                    else
+                        umma::tma_load_4d(dst + q * kChunkBytes, &tm1, 8 * (q - c0_chunks), x0 + dx,
+                                          y + dy, b, &full[s]);
+                }
+                if (++s == kStages) {
+                    s = 0;
+                    phase ^= 1u;
+                }
+            }
+        }
+        if (!ok) atomicOr(P.status, 2);
+    } else if (warp == 1 && lane == 0) {
+        bool ok = umma::mbar_wait(&wbar, 0);
+        const uint32_t idesc = umma::idesc_bf16_f32(kTileM, P.N);
+        const uint32_t lbo_b = (uint32_t)(P.N / 8) * 128u;
+        const uint32_t w0 = umma::smem_u32(smem + P.smem_w);
+        const uint32_t a0 = umma::smem_u32(smem + P.smem_a);
+        int s = 0, acc = 0;
+        uint32_t phase = 0, acc_phase = 0;
+        for (int tile = blockIdx.x; tile < P.n_tiles && ok; tile += gridDim.x) {
+            if (!umma::mbar_wait(&acc_empty[acc], acc_phase ^ 1u)) {
+                ok = false;
+                break;
+            }
+            umma::fence_after_sync();
+            const uint32_t d = tmem + (uint32_t)(acc * P.N);
+            for (int t = 0; t < 9 && ok; ++t) {
+                if (!umma::mbar_wait(&full[s], phase)) {
+                    ok = false;
+                    break;
+                }
+                umma::fence_after_sync();
+                const uint32_t sa = a0 + (uint32_t)s * chunks * kChunkBytes;
+                for (int m = 0; m < chunks / 2; ++m) {
+                    const uint64_t ad = umma::smem_desc(sa + 2u * m * kChunkBytes, kChunkBytes, 128);
+                    const uint64_t bd =
+                        umma::smem_desc(w0 + (uint32_t)(t * chunks + 2 * m) * lbo_b, lbo_b, 128);
+                    umma::mma_bf16(d, ad, bd, idesc, (t > 0 || m > 0) ? 1u : 0u);
+                }
+                umma::commit(&empty[s]);
+                if (++s == kStages) {
+                    s = 0;
+                    phase ^= 1u;
+                }
+            }
+            umma::commit(&acc_full[acc]);
+            if (++acc == 2) {
+                acc = 0;
+                acc_phase ^= 1u;
+            }
+        }
+        if (!ok) atomicOr(P.status, 2);
+    } else if (warp >= 2) {
+        const int quarter = warp & 3;  // TMEM lanes this warp may read
+        const int row = quarter * 32 + lane;
+        int acc = 0;
+        uint32_t acc_phase = 0;
+        for (int tile = blockIdx.x; tile < P.n_tiles; tile += gridDim.x) {
+            bool ok = true;
+            if (lane == 0) ok = umma::mbar_wait(&acc_full[acc], acc_phase);
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) {
+                if (lane == 0) atomicOr(P.status, 2);
+                break;
+            }
+            umma::fence_after_sync();
+            const int tx = tile % P.tiles_x, rest = tile / P.tiles_x;
+            const int y = rest % P.H, b = rest / P.H;
+            const int x = tx * kTileM + row;
+            const bool inside = x < P.W;
+            const size_t pix = ((size_t)b * P.H + y) * P.W + (inside ? x : 0);
+            float head = P.head_b;
+            for (int c = 0; c < P.N; c += 16) {
+                float v[16];
+                umma::tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * P.N + c), v);
+                if (!inside) continue;
+                if (P.bias)
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] += P.bias[c + j];
+                if (P.relu)
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] = v[j] > 0.0f ? v[j] : 0.0f;
+                if (P.gate) {
+                    const uint4* g = reinterpret_cast<const uint4*>(P.gate + pix * P.N + c);
+                    const uint4 g0 = g[0], g1 = g[1];
+                    const uint32_t gw[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const uint16_t h = (uint16_t)(gw[j / 2] >> (16 * (j & 1)));
+                        if (!(bf16_to_f(h) > 0.0f)) v[j] = 0.0f;
+                    }
+                }
+                if (P.head_out)
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) head += P.head_w[c + j] * v[j];
+                uint32_t packed[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    packed[j] = (uint32_t)f_to_bf16(v[2 * j]) | ((uint32_t)f_to_bf16(v[2 * j + 1]) << 16);
+                uint16_t* dst = nullptr;
+                size_t off = 0;
+                if (c < P.n0 && P.out0) {
+                    dst = P.out0;
+                    off = pix * P.n0 + c;
+                } else if (c >= P.n0 && P.out1) {
+                    dst = P.out1;
+                    off = pix * (P.N - P.n0) + (c - P.n0);
+                }
+                if (dst) {
+                    uint4* o = reinterpret_cast<uint4*>(dst + off);
+                    o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                }
+            }
+            if (inside && P.head_out) P.head_out[pix] = head;
+            umma::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) umma::mbar_arrive(&acc_empty[acc]);
+            if (++acc == 2) {
+                acc = 0;
+                acc_phase ^= 1u;
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 1) umma::tmem_dealloc(tmem, P.tmem_cols);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 4-D map of an NHWC bf16 tensor with an {8 channels, 128 pixels} box.
+bool encode_nhwc(CUtensorMap* map, const void* base, int B, int H, int W, int C) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    cuuint32_t box[4] = {8, (cuuint32_t)kTileM, 1, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box,
+              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int num_sms_dev() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+}  // namespace
+
+}  // namespace natrix
+
+extern "C" int natrix_nn_conv3x3(const natrix_nn_conv* c, void* stream) {
+    using namespace natrix;
+    if (!c || !c->src0 || !c->wpack)
+        return set_last_error(NATRIX_EINVAL, "conv: NULL source or weights");
+    if (c->c0 % 8 || c->c1 % 8 || c->c0 < 8 || c->N % 16 || c->N < 16 || c->N > 128 ||
+        c->n0 % 16 || c->n0 > c->N || c->B < 1 || c->H < 1 || c->W < 1 || (c->c1 && !c->src1))
+        return set_last_error(NATRIX_EINVAL, "conv: input channels must be multiples of 8, "
+                                             "outputs multiples of 16 up to 128");
+    if (c->head_out && c->N > 16)
+        return set_last_error(NATRIX_EINVAL, "conv: the fused head takes 16 channels");
+    ConvParams P{};
+    P.B = c->B;
+    P.H = c->H;
+    P.W = c->W;
+    P.c0 = c->c0;
+    P.c1 = c->c1;
+    P.ctot = (c->c0 + c->c1 + 15) / 16 * 16;
+    P.N = c->N;
+    P.wpack = c->wpack;
+    P.bias = c->bias;
+    P.relu = c->relu;
+    P.gate = c->gate;
+    P.out0 = c->out0;
+    P.n0 = c->out1 ? c->n0 : c->N;
+    P.out1 = c->out1;
+    P.head_w = c->head_w;
+    P.head_b = c->head_b;
+    P.head_out = c->head_out;
+    P.status = c->status;
+    P.tiles_x = (c->W + kTileM - 1) / kTileM;
+    P.n_tiles = P.tiles_x * c->H * c->B;
+    const uint32_t wbytes = (uint32_t)P.N * 9u * (uint32_t)P.ctot * 2u;
+    P.smem_w = 0;
+    P.smem_a = (wbytes + 1023u) / 1024u * 1024u;
+    const uint32_t abytes = (uint32_t)kStages * (P.ctot / 8) * kChunkBytes;
+    const uint32_t smem = P.smem_a + abytes;
+    uint32_t cols = 32;
+    while (cols < 2u * (uint32_t)P.N) cols *= 2;
+    P.tmem_cols = cols;
+    if (smem > 200u * 1024u)
+        return set_last_error(NATRIX_EINVAL, "conv: weights + activation ring exceed shared memory");
+    if (!P.status) return set_last_error(NATRIX_EINVAL, "conv: status word required");
+    CUtensorMap tm0, tm1;
+    if (!encode_nhwc(&tm0, c->src0, c->B, c->H, c->W, c->c0) ||
+        !encode_nhwc(&tm1, c->src1 ? c->src1 : c->src0, c->B, c->H, c->W,
+                     c->src1 ? c->c1 : c->c0))
+        return set_last_error(NATRIX_ECUDA, "conv: tensor map encoding failed");
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024) != cudaSuccess)
+            return set_last_error(NATRIX_ECUDA, "conv: shared memory attribute");
+        attr = true;
+    }
+    const int grid = P.n_tiles < num_sms_dev() ? P.n_tiles : num_sms_dev();
+    k_conv3x3_tc<<<grid, 192, smem, reinterpret_cast<cudaStream_t>(stream)>>>(tm0, tm1, P);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_last_error(NATRIX_ECUDA, cudaGetErrorString(e));
+    return NATRIX_OK;
+}

@@ -1,0 +1,634 @@
+// U-Net warm start: every kernel but the tensor-core convolutions
+// (unet_conv.cu).  Activations are NHWC bf16; gradients of activations bf16;
+// parameters, their gradients and the Adam state FP32.
+//
+//  * pack_weights: FP32 [cout][cin][3][3] master weights -> bf16 B operand in
+//    the tcgen05 SWIZZLE_NONE K-major layout (forward: rows = cout, K =
+//    (tap, cin); input gradient: rows = cin, K = (tap, cout), taps flipped).
+//  * wgrad: dW[co][ci][t] = sum_p dZ[p][co] * X[p + off(t)][ci] and
+//    db[co] = sum_p dZ[p][co] on CUDA cores: each CTA owns one tap and a
+//    slice of the pixels, accumulates in registers, then one atomic per weight.
+//  * prep / pool / upsample (and their gradients with the ReLU gate), head
+//    gradient, loss + gradient, Adam.
+//  * FP64 conjugate gradients on the pressure operator of the solver
+//    (shader.Poisson.comp:17-38 fixed point restricted to fluid cells), one
+//    independent system per image, for the training targets.
+#include <cuda_runtime.h>
+
+#include "../../include/natrix.h"
+#include "../../include/natrix_nn.h"
+#include "kernels.cuh"
+
+namespace natrix {
+
+namespace {
+
+__device__ __forceinline__ float bf(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
+__device__ __forceinline__ uint16_t tobf(float f) {
+    uint32_t u = __float_as_uint(f);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// ------------------------------------------------------------------ weights
+// element (row n, K index k) of an N x K operand -> byte offset in the layout
+__device__ __forceinline__ size_t core_off(int n, int k, int N) {
+    const size_t lbo = (size_t)(N / 8) * 128;
+    return (size_t)(n / 8) * 128 + (size_t)(k / 8) * lbo + (n % 8) * 16 + (k % 8) * 2;
+}
+
+__global__ void k_pack(const float* __restrict__ w, int cout, int cin, int rows, int kc,
+                       int dgrad, uint16_t* __restrict__ out) {
+    // rows x (9 * kc) operand; forward: rows = cout (padded), kc = cin padded;
+    // dgrad: rows = cin (padded), kc = cout padded
+    const long total = (long)rows * 9 * kc;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total;
+         i += (long)gridDim.x * blockDim.x) {
+        const int n = (int)(i / (9 * kc));
+        const int k = (int)(i % (9 * kc));
+        const int t = k / kc, c = k % kc;
+        float v = 0.0f;
+        if (!dgrad) {
+            if (n < cout && c < cin) v = w[((size_t)n * cin + c) * 9 + t];
+        } else {
+            if (n < cin && c < cout) v = w[((size_t)c * cin + n) * 9 + (8 - t)];
+        }
+        out[core_off(n, k, rows) / 2] = tobf(v);
+    }
+}
+
+// -------------------------------------------------------------------- wgrad
+// grid = (9 taps, pixel slices); block = 256 threads, each owning a 4 x 4
+// register block of (co, ci) pairs; PIX pixels staged in shared memory.
+constexpr int WG_PIX = 32;
+
+__global__ void __launch_bounds__(256)
+    k_wgrad(const uint16_t* __restrict__ dz, int cout, const uint16_t* __restrict__ x0, int c0,
+            const uint16_t* __restrict__ x1, int c1, int B, int H, int W, float* __restrict__ dw,
+            float* __restrict__ db) {
+    const int cin = c0 + c1;
+    const int t = blockIdx.x, dy = t / 3 - 1, dx = t % 3 - 1;
+    extern __shared__ float sm[];
+    float* sdz = sm;                        // WG_PIX x cout
+    float* sx = sm + WG_PIX * cout;         // WG_PIX x cin
+    const int co_blocks = (cout + 3) / 4, ci_blocks = (cin + 3) / 4;
+    const int pairs = co_blocks * ci_blocks;
+    float acc[4][4];
+    float bacc[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0f;
+    const long npix = (long)B * H * W;
+    const long per = (npix + gridDim.y - 1) / gridDim.y;
+    const long p0 = (long)blockIdx.y * per, p1 = p0 + per < npix ? p0 + per : npix;
+    // thread -> register block (several passes when pairs > 256)
+    for (int pb = threadIdx.x; pb - threadIdx.x < pairs; pb += 256) {
+        const bool mine = pb < pairs;
+        const int cob = mine ? pb / ci_blocks : 0, cib = mine ? pb % ci_blocks : 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            bacc[a] = 0.0f;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = 0.0f;
+        }
+        for (long base = p0; base < p1; base += WG_PIX) {
+            __syncthreads();
+            for (int i = threadIdx.x; i < WG_PIX * cout; i += 256) {
+                const long p = base + i / cout;
+                sdz[i] = p < p1 ? bf(dz[p * cout + i % cout]) : 0.0f;
+            }
+            for (int i = threadIdx.x; i < WG_PIX * cin; i += 256) {
+                const long p = base + i / cin;
+                const int c = i % cin;
+                float v = 0.0f;
+                if (p < p1) {
+                    const int xx = (int)(p % W), yy = (int)((p / W) % H);
+                    const long bb = p / ((long)W * H);
+                    const int sx_ = xx + dx, sy_ = yy + dy;
+                    if (sx_ >= 0 && sx_ < W && sy_ >= 0 && sy_ < H) {
+                        const long q = (bb * H + sy_) * W + sx_;
+                        v = c < c0 ? bf(x0[q * c0 + c]) : bf(x1[q * c1 + (c - c0)]);
+                    }
+                }
+                sx[i] = v;
+            }
+            __syncthreads();
+            if (mine) {
+                const int np = (int)(p1 - base < WG_PIX ? p1 - base : WG_PIX);
+                for (int k = 0; k < np; ++k) {
+                    float g[4], xv[4];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        const int co = cob * 4 + a;
+                        g[a] = co < cout ? sdz[k * cout + co] : 0.0f;
+                    }
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) {
+                        const int ci = cib * 4 + b;
+                        xv[b] = ci < cin ? sx[k * cin + ci] : 0.0f;
+                    }
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        bacc[a] += g[a];
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) acc[a][b] += g[a] * xv[b];
+                    }
+                }
+            }
+        }
+        if (mine) {
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const int co = cob * 4 + a;
+                if (co >= cout) continue;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const int ci = cib * 4 + b;
+                    if (ci < cin) atomicAdd(dw + ((size_t)co * cin + ci) * 9 + t, acc[a][b]);
+                }
+                if (db && t == 4 && cib == 0) atomicAdd(db + co, bacc[a]);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------- elementwise
+// x = [div / scale, obstacle, 0 x 6] (8-channel NHWC bf16)
+__global__ void k_prep(const float* __restrict__ div, const uint8_t* __restrict__ mask,
+                       const float* __restrict__ inv_scale, int B, int H, int W, int pitch,
+                       uint16_t* __restrict__ x) {
+    const long n = (long)B * H * W;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const long b = i / ((long)H * W);
+        const long r = i % ((long)H * W);
+        const long src = b * (long)H * pitch + (r / W) * pitch + r % W;
+        const float d = div[src] * inv_scale[b];
+        const float m = mask && mask[src] ? 1.0f : 0.0f;
+        uint4 v = make_uint4((uint32_t)tobf(d) | ((uint32_t)tobf(m) << 16), 0, 0, 0);
+        *reinterpret_cast<uint4*>(x + i * 8) = v;
+    }
+}
+
+// 2x2 average pooling, stride 2 (H, W even)
+__global__ void k_pool(const uint16_t* __restrict__ in, int B, int H, int W, int C,
+                       uint16_t* __restrict__ out) {
+    const int Ho = H / 2, Wo = W / 2;
+    const long n = (long)B * Ho * Wo * C;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long p = i / C;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
+        const long b = p / ((long)Wo * Ho);
+        const long q = (b * H + 2 * y) * W + 2 * x;
+        const float s = bf(in[q * C + c]) + bf(in[(q + 1) * C + c]) + bf(in[(q + W) * C + c]) +
+                        bf(in[(q + W + 1) * C + c]);
+        out[i] = tobf(0.25f * s);
+    }
+}
+
+// nearest upsampling x2
+__global__ void k_up(const uint16_t* __restrict__ in, int B, int H, int W, int C,
+                     uint16_t* __restrict__ out) {
+    const int Ho = 2 * H, Wo = 2 * W;
+    const long n = (long)B * Ho * Wo * C;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long p = i / C;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
+        const long b = p / ((long)Wo * Ho);
+        out[i] = in[(((b * H + y / 2) * W) + x / 2) * C + c];
+    }
+}
+
+// gradient of nearest upsampling (sum of the 4 children), times (gate > 0)
+__global__ void k_up_back(const uint16_t* __restrict__ dup, int B, int H, int W, int C,
+                          const uint16_t* __restrict__ gate, uint16_t* __restrict__ out) {
+    const long n = (long)B * H * W * C;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long p = i / C;
+        const int x = (int)(p % W), y = (int)((p / W) % H);
+        const long b = p / ((long)W * H);
+        const long q = (b * 2 * H + 2 * y) * (2 * W) + 2 * x;
+        const float s = bf(dup[q * C + c]) + bf(dup[(q + 1) * C + c]) +
+                        bf(dup[(q + 2 * W) * C + c]) + bf(dup[(q + 2 * W + 1) * C + c]);
+        out[i] = bf(gate[i]) > 0.0f ? tobf(s) : (uint16_t)0;
+    }
+}
+
+// (skip + gradient of 2x2 average pooling) times (gate > 0)
+__global__ void k_pool_back(const uint16_t* __restrict__ skip, const uint16_t* __restrict__ dq,
+                            int B, int H, int W, int C, const uint16_t* __restrict__ gate,
+                            uint16_t* __restrict__ out) {
+    const long n = (long)B * H * W * C;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long p = i / C;
+        const int x = (int)(p % W), y = (int)((p / W) % H);
+        const long b = p / ((long)W * H);
+        const long q = (b * (H / 2) + y / 2) * (W / 2) + x / 2;
+        const float s = bf(skip[i]) + 0.25f * bf(dq[q * C + c]);
+        out[i] = bf(gate[i]) > 0.0f ? tobf(s) : (uint16_t)0;
+    }
+}
+
+// head (1x1, 16 -> 1) gradient: dWh += dp * d1, dbh += dp, dZ = dp * Wh * (d1 > 0)
+__global__ void __launch_bounds__(256)
+    k_head_back(const float* __restrict__ dp, const uint16_t* __restrict__ d1, int C, long n,
+                const float* __restrict__ hw, float* __restrict__ dhw, float* __restrict__ dhb,
+                uint16_t* __restrict__ dz) {
+    __shared__ float s[16 + 1];
+    if (threadIdx.x < 17) s[threadIdx.x] = 0.0f;
+    __syncthreads();
+    float acc[16];
+    float accb = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) acc[c] = 0.0f;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const float g = dp[i];
+        accb += g;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            const float a = bf(d1[i * 16 + c]);
+            acc[c] += g * a;
+            dz[i * 16 + c] = a > 0.0f ? tobf(g * hw[c]) : (uint16_t)0;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+        const float v = warp_sum_f(acc[c]);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&s[c], v);
+    }
+    const float vb = warp_sum_f(accb);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&s[16], vb);
+    __syncthreads();
+    if (threadIdx.x < 16) atomicAdd(dhw + threadIdx.x, s[threadIdx.x]);
+    if (threadIdx.x == 0) atomicAdd(dhb, s[16]);
+}
+
+// -------------------------------------------------------------------- loss
+// Per image b (fluid cells f, mask == 0):
+//   pressure term  Lp = mean_f (e - mean_f e)^2,  e = p - target (both in the
+//                  divergence-normalised units of the network)
+//   residual term  Lr = sum_f r^2 / sum_f b^2,    r = b - A p (the sweep's operator)
+// loss = sum_b (Lp + lambda Lr) / B.  dp is the gradient of that loss.
+// Pass 1 accumulates per-image sums; pass 2 writes dp.
+__device__ __forceinline__ void nbr_sub(const uint8_t* mask, int x, int y, int W, int H, int P,
+                                        size_t base, bool& sl, bool& sr, bool& sb, bool& st) {
+    sl = x == 0 || (mask && mask[base + (size_t)y * P + x - 1]);
+    sr = x == W - 1 || (mask && mask[base + (size_t)y * P + x + 1]);
+    sb = y == 0 || (mask && mask[base + (size_t)(y - 1) * P + x]);
+    st = y == H - 1 || (mask && mask[base + (size_t)(y + 1) * P + x]);
+}
+
+// (A p)_c with the neighbour rule of the sweep; p dense (image stride H*W)
+__device__ __forceinline__ float apply_op(const float* p, size_t pb, const uint8_t* mask,
+                                          size_t mb, int x, int y, int W, int H, int P) {
+    bool sl, sr, sb, st;
+    nbr_sub(mask, x, y, W, H, P, mb, sl, sr, sb, st);
+    const size_t c = pb + (size_t)y * W + x;
+    const float pc = p[c];
+    const float l = sl ? pc : p[c - 1], r = sr ? pc : p[c + 1];
+    const float b = sb ? pc : p[c - W], t = st ? pc : p[c + W];
+    return (((l + r) + b) + t) - 4.0f * pc;
+}
+
+__global__ void __launch_bounds__(256)
+    k_loss_sums(const float* __restrict__ p, const float* __restrict__ target,
+                const float* __restrict__ div, const float* __restrict__ inv_scale,
+                const uint8_t* __restrict__ mask, int H, int W, int P,
+                double* __restrict__ sums /* B x 6: n, se, see, srr, sbb, pad */) {
+    const int b = blockIdx.y;
+    const size_t pb = (size_t)b * H * W, mb = (size_t)b * H * P;
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < (long)H * W;
+         i += (long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % W), y = (int)(i / W);
+        if (mask && mask[mb + (size_t)y * P + x]) continue;
+        const float e = p[pb + i] - target[pb + i];
+        const float bb = div[mb + (size_t)y * P + x] * inv_scale[b];
+        const float r = bb - apply_op(p, pb, mask, mb, x, y, W, H, P);
+        acc[0] += 1.0;
+        acc[1] += e;
+        acc[2] += (double)e * e;
+        acc[3] += (double)r * r;
+        acc[4] += (double)bb * bb;
+    }
+    for (int j = 0; j < 5; ++j) {
+        const double v = warp_sum_d(acc[j]);
+        if ((threadIdx.x & 31) == 0) atomicAdd(sums + b * 6 + j, v);
+    }
+}
+
+// residual r on fluid cells (0 elsewhere), for the gradient of the residual term
+__global__ void k_loss_resid(const float* __restrict__ p, const float* __restrict__ div,
+                             const float* __restrict__ inv_scale, const uint8_t* __restrict__ mask,
+                             int B, int H, int W, int P, float* __restrict__ r) {
+    const long n = (long)B * H * W;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / ((long)H * W));
+        const long k = i % ((long)H * W);
+        const int x = (int)(k % W), y = (int)(k / W);
+        const size_t pb = (size_t)b * H * W, mb = (size_t)b * H * P;
+        if (mask && mask[mb + (size_t)y * P + x]) {
+            r[i] = 0.0f;
+            continue;
+        }
+        const float bb = div[mb + (size_t)y * P + x] * inv_scale[b];
+        r[i] = bb - apply_op(p, pb, mask, mb, x, y, W, H, P);
+    }
+}
+
+// dp = (2/(B n)) (e - mean e) on fluid cells  -  lambda (2/(B sbb)) A r
+// (A is symmetric on the fluid cells, where r is supported)
+__global__ void k_loss_grad(const float* __restrict__ p, const float* __restrict__ target,
+                            const float* __restrict__ r, const uint8_t* __restrict__ mask,
+                            const double* __restrict__ sums, float lambda, int B, int H, int W,
+                            int P, float* __restrict__ dp) {
+    const long n = (long)B * H * W;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / ((long)H * W));
+        const long k = i % ((long)H * W);
+        const int x = (int)(k % W), y = (int)(k / W);
+        const size_t pb = (size_t)b * H * W, mb = (size_t)b * H * P;
+        if (mask && mask[mb + (size_t)y * P + x]) {
+            dp[i] = 0.0f;
+            continue;
+        }
+        const double* s = sums + b * 6;
+        const double nf = s[0] > 0 ? s[0] : 1.0;
+        const float mean_e = (float)(s[1] / nf);
+        const float e = p[i] - target[i] - mean_e;
+        const float g1 = (float)(2.0 / (B * nf)) * e;
+        const float ar = apply_op(r, pb, mask, mb, x, y, W, H, P);
+        const float g2 = -lambda * (float)(2.0 / (B * (s[4] > 0 ? s[4] : 1.0))) * ar;
+        dp[i] = g1 + g2;
+    }
+}
+
+// --------------------------------------------------------------------- adam
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, long n, float lr, float b1, float b2, float eps,
+                       float c1, float c2) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float mh = mi / c1, vh = vi / c2;
+        w[i] -= lr * mh / (sqrtf(vh) + eps);
+    }
+}
+
+// ---------------------------------------------------------- FP64 CG solver
+// Dense per-image vectors (stride H*W); mask pitch P (bytes per row).
+__global__ void k_cg_apply(const double* __restrict__ x, const uint8_t* __restrict__ mask, int B,
+                           int H, int W, int P, double* __restrict__ y) {
+    const long n = (long)B * H * W;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / ((long)H * W));
+        const long k = i % ((long)H * W);
+        const int xx = (int)(k % W), yy = (int)(k / W);
+        const size_t mb = (size_t)b * H * P;
+        if (mask && mask[mb + (size_t)yy * P + xx]) {
+            y[i] = 0.0;
+            continue;
+        }
+        bool sl, sr, sb, st;
+        nbr_sub(mask, xx, yy, W, H, P, mb, sl, sr, sb, st);
+        const double c = x[i];
+        const double l = sl ? c : x[i - 1], r = sr ? c : x[i + 1];
+        const double bo = sb ? c : x[i - W], t = st ? c : x[i + W];
+        // negated so the operator is positive semi-definite for CG
+        y[i] = -((((l + r) + bo) + t) - 4.0 * c);
+    }
+}
+
+// out[b] += sum over image b of a*b (fluid cells only when mask given)
+__global__ void __launch_bounds__(256)
+    k_cg_dot(const double* __restrict__ a, const double* __restrict__ c,
+             const uint8_t* __restrict__ mask, int H, int W, int P, double* __restrict__ out) {
+    const int b = blockIdx.y;
+    const size_t base = (size_t)b * H * W, mb = (size_t)b * H * P;
+    double acc = 0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < (long)H * W;
+         i += (long)gridDim.x * blockDim.x) {
+        if (mask && mask[mb + (i / W) * P + i % W]) continue;
+        acc += a[base + i] * c[base + i];
+    }
+    acc = warp_sum_d(acc);
+    __shared__ double s[8];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int k = 0; k < 8; ++k) t += s[k];
+        atomicAdd(out + b, t);
+    }
+}
+
+// y = x + alpha[b] * y_scale * d   (per image coefficient; sign selects +/-)
+__global__ void k_cg_axpy(double* __restrict__ y, const double* __restrict__ d,
+                          const double* __restrict__ num, const double* __restrict__ den,
+                          double sign, int B, long per) {
+    const long n = (long)B * per;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / per);
+        const double a = den[b] != 0.0 ? num[b] / den[b] : 0.0;
+        y[i] += sign * a * d[i];
+    }
+}
+
+// d = r + (rr_new / rr_old) d
+__global__ void k_cg_dir(double* __restrict__ d, const double* __restrict__ r,
+                         const double* __restrict__ rr_new, const double* __restrict__ rr_old,
+                         int B, long per) {
+    const long n = (long)B * per;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / per);
+        const double beta = rr_old[b] != 0.0 ? rr_new[b] / rr_old[b] : 0.0;
+        d[i] = r[i] + beta * d[i];
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+int launch_status() {
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? NATRIX_OK : set_last_error(NATRIX_ECUDA, cudaGetErrorString(e));
+}
+
+}  // namespace natrix
+
+using namespace natrix;
+
+extern "C" {
+
+int natrix_nn_pack(const float* w, int32_t cout, int32_t cin, int32_t rows, int32_t kc,
+                   int32_t dgrad, uint16_t* out, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long total = (long)rows * 9 * kc;
+    k_pack<<<blocks(total, 256) < 4096 ? blocks(total, 256) : 4096, 256, 0, st>>>(
+        w, cout, cin, rows, kc, dgrad, out);
+    return launch_status();
+}
+
+int natrix_nn_wgrad(const uint16_t* dz, int32_t cout, const uint16_t* x0, int32_t c0,
+                    const uint16_t* x1, int32_t c1, int32_t B, int32_t H, int32_t W, float* dw,
+                    float* db, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long npix = (long)B * H * W;
+    int slices = (int)((npix + 4095) / 4096);
+    slices = slices < 1 ? 1 : (slices > 256 ? 256 : slices);
+    const size_t smem = (size_t)WG_PIX * (cout + c0 + c1) * sizeof(float);
+    k_wgrad<<<dim3(9, slices), 256, smem, st>>>(dz, cout, x0, c0, x1, c1, B, H, W, dw, db);
+    return launch_status();
+}
+
+int natrix_nn_prep(const float* div, const uint8_t* mask, const float* inv_scale, int32_t B,
+                   int32_t H, int32_t W, int32_t pitch, uint16_t* x, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long n = (long)B * H * W;
+    k_prep<<<blocks(n, 256) < 8192 ? blocks(n, 256) : 8192, 256, 0, st>>>(div, mask, inv_scale, B,
+                                                                          H, W, pitch, x);
+    return launch_status();
+}
+
+int natrix_nn_pool(const uint16_t* in, int32_t B, int32_t H, int32_t W, int32_t C, uint16_t* out,
+                   void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long n = (long)B * (H / 2) * (W / 2) * C;
+    k_pool<<<blocks(n, 256) < 8192 ? blocks(n, 256) : 8192, 256, 0, st>>>(in, B, H, W, C, out);
+    return launch_status();
+}
+
+int natrix_nn_up(const uint16_t* in, int32_t B, int32_t H, int32_t W, int32_t C, uint16_t* out,
+                 void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long n = (long)B * 4 * H * W * C;
+    k_up<<<blocks(n, 256) < 8192 ? blocks(n, 256) : 8192, 256, 0, st>>>(in, B, H, W, C, out);
+    return launch_status();
+}
+
+int natrix_nn_up_back(const uint16_t* dup, int32_t B, int32_t H, int32_t W, int32_t C,
+                      const uint16_t* gate, uint16_t* out, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long n = (long)B * H * W * C;
+    k_up_back<<<blocks(n, 256) < 8192 ? blocks(n, 256) : 8192, 256, 0, st>>>(dup, B, H, W, C,
+                                                                            gate, out);
+    return launch_status();
+}
+
+int natrix_nn_pool_back(const uint16_t* skip, const uint16_t* dq, int32_t B, int32_t H, int32_t W,
+                        int32_t C, const uint16_t* gate, uint16_t* out, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long n = (long)B * H * W * C;
+    k_pool_back<<<blocks(n, 256) < 8192 ? blocks(n, 256) : 8192, 256, 0, st>>>(skip, dq, B, H, W,
+                                                                              C, gate, out);
+    return launch_status();
+}
+
+int natrix_nn_head_back(const float* dp, const uint16_t* d1, int32_t C, int64_t n,
+                        const float* hw, float* dhw, float* dhb, uint16_t* dz, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (C != 16) return set_last_error(NATRIX_EINVAL, "head: 16 channels expected");
+    k_head_back<<<blocks(n, 256) < 2048 ? blocks(n, 256) : 2048, 256, 0, st>>>(dp, d1, C, n, hw,
+                                                                              dhw, dhb, dz);
+    return launch_status();
+}
+
+int natrix_nn_loss(const float* p, const float* target, const float* div, const float* inv_scale,
+                   const uint8_t* mask, int32_t B, int32_t H, int32_t W, int32_t P, float lambda,
+                   double* sums, float* r, float* dp, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(sums, 0, (size_t)B * 6 * sizeof(double), st) != cudaSuccess)
+        return launch_status();
+    const long per = (long)H * W;
+    const unsigned bx = blocks(per, 256) < 256 ? blocks(per, 256) : 256;
+    k_loss_sums<<<dim3(bx, B), 256, 0, st>>>(p, target, div, inv_scale, mask, H, W, P, sums);
+    const long n = (long)B * per;
+    const unsigned g = blocks(n, 256) < 8192 ? blocks(n, 256) : 8192;
+    if (dp) {
+        k_loss_resid<<<g, 256, 0, st>>>(p, div, inv_scale, mask, B, H, W, P, r);
+        k_loss_grad<<<g, 256, 0, st>>>(p, target, r, mask, sums, lambda, B, H, W, P, dp);
+    }
+    return launch_status();
+}
+
+int natrix_nn_adam(float* w, const float* g, float* m, float* v, int64_t n, float lr, float b1,
+                   float b2, float eps, int32_t step, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    k_adam<<<blocks(n, 256) < 4096 ? blocks(n, 256) : 4096, 256, 0, st>>>(w, g, m, v, n, lr, b1, b2,
+                                                                          eps, c1, c2);
+    return launch_status();
+}
+
+int natrix_nn_cg_apply(const double* x, const uint8_t* mask, int32_t B, int32_t H, int32_t W,
+                       int32_t P, double* y, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long n = (long)B * H * W;
+    k_cg_apply<<<blocks(n, 256) < 16384 ? blocks(n, 256) : 16384, 256, 0, st>>>(x, mask, B, H, W,
+                                                                                P, y);
+    return launch_status();
+}
+
+int natrix_nn_cg_dot(const double* a, const double* c, const uint8_t* mask, int32_t B, int32_t H,
+                     int32_t W, int32_t P, double* out, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(out, 0, (size_t)B * sizeof(double), st) != cudaSuccess)
+        return launch_status();
+    const long per = (long)H * W;
+    const unsigned bx = blocks(per, 256) < 128 ? blocks(per, 256) : 128;
+    k_cg_dot<<<dim3(bx, B), 256, 0, st>>>(a, c, mask, H, W, P, out);
+    return launch_status();
+}
+
+int natrix_nn_cg_axpy(double* y, const double* d, const double* num, const double* den,
+                      double sign, int32_t B, int64_t per, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long n = (long)B * per;
+    k_cg_axpy<<<blocks(n, 256) < 16384 ? blocks(n, 256) : 16384, 256, 0, st>>>(y, d, num, den, sign,
+                                                                               B, per);
+    return launch_status();
+}
+
+int natrix_nn_cg_dir(double* d, const double* r, const double* rr_new, const double* rr_old,
+                     int32_t B, int64_t per, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long n = (long)B * per;
+    k_cg_dir<<<blocks(n, 256) < 16384 ? blocks(n, 256) : 16384, 256, 0, st>>>(d, r, rr_new, rr_old,
+                                                                              B, per);
+    return launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,295 @@
+"""U-Net warm start on the GPU: tensor-core convolution forward / input
+gradient and CUDA-core weight gradient against torch CPU float64, the whole
+network's gradients against the CPU reference network (oracle/unet_ref.py),
+Adam against its formula, the FP64 CG targets against the oracle's residual,
+training progress, and what the trained warm start gains over zero start."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+BF16_RTOL = 1.6e-2  # two bf16 ulps: the GPU rounds its FP32 accumulator once
+
+
+def bf16(t):
+    import torch
+
+    return t.to(torch.bfloat16)
+
+
+def as_u16(t):
+    import torch
+
+    return t.to(torch.bfloat16).view(torch.int16)
+
+
+def from_u16(t):
+    import torch
+
+    return t.view(torch.bfloat16).double()
+
+
+def close(got, want, rtol=BF16_RTOL, what=""):
+    got = got.double().cpu()
+    want = want.double().cpu()
+    scale = float(want.abs().max()) or 1.0
+    err = float((got - want).abs().max())
+    assert err <= rtol * scale, f"{what}: max |err| {err:.3g} > {rtol} x {scale:.3g}"
+
+
+CONV_CASES = [
+    # B, H, W, c0, c1, N
+    (2, 6, 200, 16, 0, 32),
+    (1, 5, 128, 64, 32, 32),
+    (2, 4, 64, 8, 0, 16),
+    (1, 3, 136, 32, 16, 48),
+    (1, 4, 96, 32, 0, 96),
+]
+
+
+@pytest.mark.parametrize("B,H,W,c0,c1,N", CONV_CASES)
+def test_conv_forward_and_input_gradient(cuda, B, H, W, c0, c1, N):
+    import torch
+    import torch.nn.functional as F
+
+    from natrix_gb300.core import warmstart as ws
+
+    g = torch.Generator().manual_seed(B * 100 + W + N)
+    cin = c0 + c1
+    x0 = bf16(torch.randn(B, H, W, c0, generator=g))
+    x1 = bf16(torch.randn(B, H, W, c1, generator=g)) if c1 else None
+    w = torch.randn(N, cin, 3, 3, generator=g) * 0.2
+    bias = torch.randn(N, generator=g) * 0.1
+    ctot = (cin + 15) // 16 * 16
+    dev = "cuda"
+    wd = w.to(dev)
+    pack = torch.zeros(N * 9 * ctot, dtype=torch.int16, device=dev)
+    ws._call("natrix_nn_pack", ws._p(wd), N, cin, N, ctot, 0, ws._p(pack), ws._s())
+    out = torch.empty(B, H, W, N, dtype=torch.int16, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    x0d = as_u16(x0.float()).to(dev)
+    x1d = as_u16(x1.float()).to(dev) if x1 is not None else None
+    bias_d = bias.to(dev)
+    c = ws.NnConv()
+    c.src0, c.c0 = ws._p(x0d), c0
+    c.src1, c.c1 = (ws._p(x1d), c1) if x1 is not None else (None, 0)
+    c.B, c.H, c.W, c.N = B, H, W, N
+    c.wpack, c.bias, c.relu = ws._p(pack), ws._p(bias_d), 1
+    c.out0, c.n0, c.status = ws._p(out), N, ws._p(status)
+    ws._call("natrix_nn_conv3x3", ctypes_byref(c), ws._s())
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    xin = torch.cat([x0, x1], -1) if x1 is not None else x0
+    xin = xin.double().permute(0, 3, 1, 2)
+    wq = bf16(w).double()
+    ref = F.relu(F.conv2d(xin, wq, bias.double(), padding=1)).permute(0, 2, 3, 1)
+    close(from_u16(out), ref, what="conv forward")
+
+    # input gradient: the same kernel with the packed transposed, flipped weights
+    dz = bf16(torch.randn(B, H, W, N, generator=g))
+    dzd = as_u16(dz.float()).to(dev)
+    nin = ctot
+    packb = torch.zeros(nin * 9 * N, dtype=torch.int16, device=dev)
+    ws._call("natrix_nn_pack", ws._p(wd), N, cin, nin, N, 1, ws._p(packb), ws._s())
+    gin = torch.empty(B, H, W, nin, dtype=torch.int16, device=dev)
+    c2 = ws.NnConv()
+    c2.src0, c2.c0, c2.src1, c2.c1 = ws._p(dzd), N, None, 0
+    c2.B, c2.H, c2.W, c2.N = B, H, W, nin
+    c2.wpack, c2.relu = ws._p(packb), 0
+    c2.out0, c2.n0, c2.status = ws._p(gin), nin, ws._p(status)
+    ws._call("natrix_nn_conv3x3", ctypes_byref(c2), ws._s())
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    want = torch.nn.grad.conv2d_input(xin.shape, wq, dz.double().permute(0, 3, 1, 2), padding=1)
+    close(from_u16(gin)[..., :cin], want.permute(0, 2, 3, 1), what="conv input gradient")
+
+
+def ctypes_byref(c):
+    import ctypes
+
+    return ctypes.byref(c)
+
+
+@pytest.mark.parametrize("B,H,W,c0,c1,cout", [(2, 8, 40, 16, 0, 32), (1, 12, 24, 64, 32, 32),
+                                              (2, 6, 16, 8, 0, 16)])
+def test_weight_gradient(cuda, B, H, W, c0, c1, cout):
+    import torch
+
+    from natrix_gb300.core import warmstart as ws
+
+    g = torch.Generator().manual_seed(7 + W)
+    cin = c0 + c1
+    x0 = bf16(torch.randn(B, H, W, c0, generator=g))
+    x1 = bf16(torch.randn(B, H, W, c1, generator=g)) if c1 else None
+    dz = bf16(torch.randn(B, H, W, cout, generator=g))
+    dw = torch.zeros(cout, cin, 3, 3, device="cuda")
+    db = torch.zeros(cout, device="cuda")
+    x0d, dzd = as_u16(x0.float()).cuda(), as_u16(dz.float()).cuda()
+    x1d = as_u16(x1.float()).cuda() if x1 is not None else None
+    ws._call("natrix_nn_wgrad", ws._p(dzd), cout, ws._p(x0d), c0, ws._p(x1d), c1 if x1 is not None else 0,
+             B, H, W, ws._p(dw), ws._p(db), ws._s())
+    torch.cuda.synchronize()
+    xin = (torch.cat([x0, x1], -1) if x1 is not None else x0).double().permute(0, 3, 1, 2)
+    want = torch.nn.grad.conv2d_weight(xin, (cout, cin, 3, 3), dz.double().permute(0, 3, 1, 2),
+                                       padding=1)
+    close(dw, want, rtol=1e-4, what="weight gradient")
+    close(db, dz.double().sum((0, 1, 2)), rtol=1e-4, what="bias gradient")
+
+
+def _small_problem(seed=0, B=2, H=32, W=48):
+    import torch
+
+    g = torch.Generator().manual_seed(seed)
+    P = (W + 31) // 32 * 32
+    div = torch.zeros(B, H, P)
+    div[:, :, :W] = torch.randn(B, H, W, generator=g) * 0.3
+    mask = torch.zeros(B, H, P, dtype=torch.uint8)
+    yy, xx = torch.meshgrid(torch.arange(H), torch.arange(W), indexing="ij")
+    for b in range(B):
+        cx, cy, r = 10 + 7 * b, 12, 4
+        mask[b, :, :W] = (((xx - cx) ** 2 + (yy - cy) ** 2) <= r * r).to(torch.uint8)
+    target = torch.randn(B, H, W, generator=g)
+    return div.cuda(), mask.cuda(), target.cuda(), P
+
+
+def test_network_gradients_match_cpu_reference(cuda):
+    import torch
+
+    from natrix_gb300.core import warmstart as ws
+    from oracle import unet_ref
+
+    B, H, W = 2, 32, 48
+    div, mask, target, P = _small_problem(B=B, H=H, W=W)
+    net = ws.UNet(seed=3)
+    # non-zero biases so every path is exercised
+    for L in net.layers:
+        L.b.copy_(torch.linspace(-0.05, 0.05, L.cout))
+    net.repack()
+    inv = ws.inv_scale_of(div, mask)
+    lam = 0.5
+    net.forward(div, mask, inv, H, W, P)
+    loss_gpu = net.loss(target, div, mask, inv, P, lam, grad=True)
+    net.zero_grad()
+    net.backward(net.acts["dp"])
+    torch.cuda.synchronize()
+    net.check_status()
+
+    params = {}
+    leaves = []
+    for L in net.layers:
+        w = unet_ref.bf16_round(L.w.double().cpu()).requires_grad_(True)
+        b = L.b.double().cpu().requires_grad_(True)
+        params[L.name] = (w, b)
+        leaves += [w, b]
+    hw = net.hw.double().cpu().requires_grad_(True)
+    hb = net.hb.double().cpu().requires_grad_(True)
+    params["head"] = (hw, hb)
+    xg = net.acts["x"].cpu().view(torch.bfloat16).double()  # the GPU's prepared input
+    x = xg[..., :2].permute(0, 3, 1, 2).contiguous()
+    w11, b11 = params["c11"]
+    p = unet_ref.forward_mirrored(params, x)
+    bnorm = (div[:, :, :W].double().cpu() * inv.double().cpu().view(B, 1, 1))
+    loss_ref = unet_ref.loss(p, target.double().cpu(), bnorm, mask[:, :, :W].cpu(), lam)
+    loss_ref.backward()
+    assert abs(loss_gpu - float(loss_ref.detach())) <= 1e-2 * abs(float(loss_ref.detach()))
+    pg = net.acts["p"].double().cpu()
+    rel_p = float((pg - p.detach()).norm() / p.detach().norm())
+    assert rel_p < 1e-2, f"prediction rel-L2 {rel_p:.3g}"
+    for L in net.layers:
+        for got, (ref_t, name) in ((L.gw, (params[L.name][0], "w")), (L.gb, (params[L.name][1], "b"))):
+            ref = ref_t.grad
+            gotc = got.double().cpu()
+            rel = float((gotc - ref).norm() / max(float(ref.norm()), 1e-30))
+            cos = float((gotc * ref).sum() / max(float(gotc.norm() * ref.norm()), 1e-30))
+            print(f"{L.name}.{name}: rel {rel:.3g} cos {cos:.6f}")
+            assert rel < 3e-2 and cos > 0.9995, f"{L.name}.{name}: rel {rel:.3g} cos {cos:.6f}"
+    rel = float((net.ghw.double().cpu() - hw.grad).norm() / float(hw.grad.norm()))
+    assert rel < 3e-2, f"head.w: rel {rel:.3g}"
+    # the loss is invariant to a constant shift of the pressure (mean-removed
+    # error; the operator annihilates constants), so d loss / d head bias = 0
+    assert abs(float(net.ghb.item())) <= 1e-5 * float(hw.grad.norm()) + 1e-7
+    assert abs(float(hb.grad.item())) <= 1e-9
+
+
+def test_adam_matches_formula(cuda):
+    import torch
+
+    from natrix_gb300.core import warmstart as ws
+
+    g = torch.Generator().manual_seed(1)
+    w0 = torch.randn(1000, generator=g)
+    grads = [torch.randn(1000, generator=g) for _ in range(3)]
+    w, m, v = w0.clone().cuda(), torch.zeros(1000, device="cuda"), torch.zeros(1000, device="cuda")
+    wr, mr, vr = w0.double().clone(), torch.zeros(1000, dtype=torch.float64), torch.zeros(1000, dtype=torch.float64)
+    lr, b1, b2, eps = 1e-3, 0.9, 0.999, 1e-8
+    for t, gr in enumerate(grads, 1):
+        ws._call("natrix_nn_adam", ws._p(w), ws._p(gr.cuda()), ws._p(m), ws._p(v), 1000, lr, b1, b2,
+                 eps, t, ws._s())
+        mr = b1 * mr + (1 - b1) * gr.double()
+        vr = b2 * vr + (1 - b2) * gr.double() ** 2
+        wr = wr - lr * (mr / (1 - b1 ** t)) / ((vr / (1 - b2 ** t)).sqrt() + eps)
+    torch.cuda.synchronize()
+    close(w, wr, rtol=1e-6, what="adam")
+
+
+def test_cg_targets_reach_tolerance(cuda, oracle):
+    import torch
+
+    from natrix_gb300.core import warmstart as ws
+
+    pairs = ws.make_pairs(64, 4, seed=5, rtol=1e-6, batch=4)
+    assert float(pairs.rel_residual.max()) <= 2e-6
+    # the oracle's residual of the same pressure system, in the solver's units
+    for k in range(pairs.n):
+        div = pairs.div[k, :, :64].cpu().numpy().astype(np.float64)
+        m = pairs.mask[k, :, :64].cpu().numpy()
+        p = pairs.target[k].cpu().numpy().astype(np.float64) / float(pairs.inv_scale[k])
+        assert oracle.relative_residual(p, div, m) <= 2e-5
+
+
+def test_training_reduces_loss_and_warm_start_gain(cuda, capsys):
+    """Train on a small set of solver-generated pairs; the loss must drop, and
+    on held-out steps the warm start (with its fallback rule) must never need
+    more sweeps than zero start; the measured gain is printed."""
+    import torch
+
+    from natrix_gb300 import FluidSimulator
+    from natrix_gb300 import workloads as wl
+    from natrix_gb300.core import warmstart as ws
+
+    size = 128
+    train = ws.make_pairs(size, 32, seed=1, rtol=1e-6, batch=32)
+    net = ws.UNet(seed=0)
+    P = train.div.shape[2]
+    losses = []
+    for it in range(150):
+        idx = torch.randint(0, train.n, (8,), generator=torch.Generator().manual_seed(it)).cuda()
+        losses.append(net.train_step(train.div[idx].contiguous(), train.mask[idx].contiguous(),
+                                     train.inv_scale[idx].contiguous(), train.target[idx].contiguous(),
+                                     size, size, P, lr=1e-3, lam=1.0))
+    net.check_status()
+    first, last = np.mean(losses[:10]), np.mean(losses[-10:])
+    assert math.isfinite(last) and last < 0.5 * first, f"loss {first:.4g} -> {last:.4g}"
+    # held-out: a fresh simulation
+    sim = FluidSimulator(size, size)
+    sim.iterations, sim.vorticity, sim.viscosity, sim.speed, sim.dissipation = 80, 0.35, 0, 5.0, 0.99
+    rng = np.random.default_rng(99)
+    obst = wl.circle_obstacles(rng, 12, size, size)
+    for _ in range(6):
+        for o in obst:
+            sim.add_circle_obstacle((float(o[0]), float(o[1])), float(o[2]))
+        mask = sim.obstacles.clone()
+        sim.add_splats(wl.gauss_splats(rng, 16, size, size, 5.0))
+        sim.update(1 / 60)
+    zero = ws.warm_start_solve(sim, None, None, rtol=1e-3, check=50, time_limit_s=60)
+    warm = ws.warm_start_solve(sim, net, mask, rtol=1e-3, check=50, time_limit_s=60)
+    with capsys.disabled():
+        print(f"\nwarm start at {size}x{size}: zero {zero['sweeps']} sweeps, network "
+              f"{warm['sweeps']} sweeps (fallback {warm['fallback']}); loss {first:.4g} -> {last:.4g}")
+    assert zero["converged"] and warm["converged"]
+    assert warm["sweeps"] <= zero["sweeps"] + 10
+    sim.destroy()
