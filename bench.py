@@ -529,20 +529,139 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_warmstart(args):
+    """Learned warm start: train on solver-generated 512x512 pairs, then time
+    the solve to relative residual 1e-4 at 512x512, 1024x1024 and 2048x2048
+    from zero and from the network's guess (with the fallback rule)."""
+    import torch
+
+    from natrix_gb300.core import warmstart as ws
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    t0 = time.perf_counter()
+    pairs = ws.make_pairs(512, args.pairs, seed=0, rtol=1e-6, batch=64)
+    t_data = time.perf_counter() - t0
+    net = ws.UNet(seed=0)
+    t0 = time.perf_counter()
+    losses = ws.train(net, pairs, steps=args.train_steps, batch=64, lr=1e-3, lam=1.0)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    # tensor-core convolution throughput: one forward of a 64 x 512 x 512 batch
+    div, mask, inv = pairs.div[:64].contiguous(), pairs.mask[:64].contiguous(), pairs.inv_scale[:64].contiguous()
+    P = div.shape[2]
+    for _ in range(2):
+        net.forward(div, mask, inv, 512, 512, P)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        net.forward(div, mask, inv, 512, 512, P)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / 5
+    flops, _ = ws.forward_cost(64, 512, 512)
+    results = {}
+    for size in (512, 1024, 2048):
+        sim, m = ws.evaluation_system(size, seed=7)
+        zero = ws.warm_start_solve(sim, None, m, rtol=1e-4, time_limit_s=args.solve_limit)
+        cnn = ws.warm_start_solve(sim, net, m, rtol=1e-4, time_limit_s=args.solve_limit)
+        sim.destroy()
+        results[str(size)] = {"zero": zero, "network": cnn,
+                              "speedup": zero["seconds"] / max(cnn["seconds"], 1e-9)}
+    peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"] \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else 1900.0
+    line = {
+        "metric": "seconds to relative residual 1e-4 at 2048x2048 (network warm start)",
+        "value": results["2048"]["network"]["seconds"], "unit": "s", "n_gpus": 1,
+        "steps": args.train_steps, "warmup": 0, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 (f32 accumulate), f32 sweeps",
+        "data": "synthetic (solver-generated pairs)",
+        "config": {"workload": "unet-warm-start", "train_grid": 512, "pairs": pairs.n,
+                   "train_steps": args.train_steps, "batch": 64, "lr": 1e-3,
+                   "cg_rel_residual_max": float(pairs.rel_residual.max()),
+                   "cg_iterations": pairs.cg_iterations},
+        "loss": {"first10": float(np.mean(losses[:10])), "last10": float(np.mean(losses[-10:]))},
+        "time": {"data_s": t_data, "train_s": t_train,
+                 "train_images_per_s": args.train_steps * 64 / t_train},
+        "conv_forward": {"batch": 64, "grid": 512, "ms": fwd_ms, "tflops": flops / fwd_ms / 1e9,
+                         "peak_tflops": peak, "frac": flops / fwd_ms / 1e9 / peak},
+        "solve": results,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_unet_forward(args):
+    """Warm-start network inference throughput: one forward pass of
+    --batch x 512 x 512 (synthetic divergence and obstacle fields) per step,
+    timed with CUDA events; roofline against the forward's algorithmic HBM
+    bytes (warmstart.forward_cost), tensor FLOP/s reported beside it."""
+    import torch
+
+    from natrix_gb300.core import warmstart as ws
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    B, H, W = args.batch, 512, 512
+    P = (W + 31) // 32 * 32
+    g = torch.Generator(device="cuda").manual_seed(0)
+    div = torch.randn(B, H, P, device="cuda", generator=g)
+    mask = (torch.rand(B, H, P, device="cuda", generator=g) < 0.05).to(torch.uint8)
+    inv = ws.inv_scale_of(div[:, :, :W], mask[:, :, :W])
+    net = ws.UNet(seed=0)
+    for _ in range(args.warmup):
+        net.forward(div, mask, inv, H, W, P)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        net.forward(div, mask, inv, H, W, P)
+    e1.record()
+    torch.cuda.synchronize()
+    net.check_status()
+    ms = e0.elapsed_time(e1) / args.steps
+    flops, nbytes = ws.forward_cost(B, H, W)
+    hbm, kind = load_peaks()
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
+    gbs = nbytes / ms / 1e6
+    print(json.dumps({
+        "metric": "U-Net forward images/s (512x512)", "value": B / ms * 1e3, "unit": "images/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 (f32 accumulate)", "data": "synthetic",
+        "config": {"workload": f"unet-forward-{B}x512x512", "batch": B,
+                   "l2": "activations of a 64-image batch exceed L2"},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": gbs / hbm, "traffic": None, "peak_kind": kind,
+                     "algorithmic_bytes": nbytes},
+        "tensor": {"tflops": flops / ms / 1e9, "peak": tc_peak, "frac": flops / ms / 1e9 / tc_peak},
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["natrix", "reference"], default="natrix")
-    ap.add_argument("--workload", choices=["large", "small", "particles", "batch"],
-                    default="large")
+    ap.add_argument("--workload", choices=["large", "small", "particles", "batch", "warmstart",
+                                           "unet-forward"], default="large")
+    ap.add_argument("--batch", type=int, default=64, help="unet-forward: images per pass")
+    ap.add_argument("--pairs", type=int, default=512, help="warmstart: training pairs")
+    ap.add_argument("--train-steps", type=int, default=400, help="warmstart: Adam steps")
+    ap.add_argument("--solve-limit", type=float, default=120.0,
+                    help="warmstart: seconds allowed per solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "natrix":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "warmstart":
+        run_warmstart(args)
+        return
+    if args.workload == "unet-forward":
+        run_unet_forward(args)
         return
     spec = make_spec(args.workload)
     if args.impl == "reference":

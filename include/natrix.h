@@ -123,6 +123,16 @@ int natrix_download(natrix_sim* sim, int32_t field, void* host, void* stream);
  * No reference counterpart. */
 int natrix_residual(natrix_sim* sim, double out[5], void* stream);
 
+/* The residual sums of natrix_residual per connected fluid region: `labels`
+ * (device, W*H int32, row-major without padding) gives each fluid cell its
+ * region in [0, n_labels) and obstacle cells a negative value; `sums`
+ * (device, n_labels x 5 doubles) receives {n, sum r, sum r^2, sum b, sum b^2}
+ * per region.  The pressure system is pure Neumann on every region, so the
+ * residual is defined up to each region's mean.  Stream-ordered, no sync.
+ * No reference counterpart. */
+int natrix_residual_regions(natrix_sim* sim, const int32_t* labels, int32_t n_labels,
+                            double* sums, void* stream);
+
 /* Run `sweeps` more Jacobi sweeps on the current pressure (no reset), with
  * the divergence and obstacles of the last step.  No reference counterpart
  * (used for residual-driven solves and warm starts). */
@@ -245,6 +255,35 @@ int natrix_set_timing(natrix_sim* sim, int32_t enable);
 
 /* Read the counters (waits for the timed events); reset = 1 zeroes them. */
 int natrix_get_stats(natrix_sim* sim, natrix_stats* out, int32_t reset);
+
+/* ---- headless visualisation (demo/shaders/demo.*) ----
+ * No graphics pipeline: each shader becomes a kernel writing a device
+ * buffer of RGBA8 pixels (4 bytes, R first).  Device pointers, stream
+ * ordered, no sync (the first call on a device also builds a 256-entry colour
+ * table and waits for it).
+ *
+ * natrix_render_density replaces demo.ComputeShader.comp:9-20 (density ->
+ * rgba8 texture, `texture`) and demo.FieldFragmentShader.frag:95-99 (the
+ * plasma(fbm(c)) colour with alpha c, `colour`) at one pixel per density
+ * cell.  `density` has `pitch` floats per row; both outputs have `out_pitch`
+ * pixels per row; either output may be NULL.  UNORM8 conversion: 0 for NaN
+ * and v <= 0, 255 for v >= 1, else round-half-even(v * 255). */
+int natrix_render_density(const float* density, int32_t width, int32_t height, int64_t pitch,
+                          uint8_t* texture, uint8_t* colour, int64_t out_pitch, void* stream);
+
+/* Arrow tiles of a win_w x win_h quiver overlay with tiles of `tile` pixels
+ * (1 <= tile <= 65536): nx = floor((win_w - 0.5) / tile) + 1, ny alike. */
+int natrix_quiver_tiles(int32_t win_w, int32_t win_h, float tile, int32_t* nx, int32_t* ny);
+
+/* demo.QuiverFragmentShader.frag: `arrows` (nx * ny float2, row-major)
+ * receives each tile's arrow in window pixels, field(tile centre) * tile *
+ * 0.4, with the shader's sampling of the velocity (width x height float2,
+ * `pitch` float2 per row); if `overlay` is not NULL it receives the
+ * win_w x win_h overlay (white, alpha 1 - clamp(distance to the arrow, 0, 1)),
+ * `overlay_pitch` pixels per row, pixel (x, y) sampled at (x + 0.5, y + 0.5). */
+int natrix_quiver(const float* velocity, int32_t width, int32_t height, int64_t pitch,
+                  int32_t win_w, int32_t win_h, float tile, float* arrows, uint8_t* overlay,
+                  int64_t overlay_pitch, void* stream);
 
 /* Largest grid, in cells, that natrix_residual_noalloc accepts (4096 x 4096). */
 #define NATRIX_NOALLOC_MAX_CELLS (4096 * 4096)

@@ -72,6 +72,7 @@ SIGNATURES = {
     "natrix_download": [_vp, _i, _vp, _vp],
     "natrix_residual": [_vp, ctypes.POINTER(ctypes.c_double), _vp],
     "natrix_jacobi": [_vp, _i, _vp],
+    "natrix_residual_regions": [_vp, _vp, _i, _vp, _vp],
     "natrix_sync": [_vp, _vp],
     "natrix_set_timing": [_vp, _i],
     "natrix_get_stats": [_vp, ctypes.POINTER(Stats), _i],
@@ -107,6 +108,10 @@ SIGNATURES = {
     "natrix_batch_launches": [_vp, _i64p, ctypes.POINTER(ctypes.c_int32)],
     "natrix_batch_sync": [_vp, _vp],
     "natrix_residual_noalloc": [_vp, _vp, _vp, _i, _i, ctypes.c_int64, _vp, _vp],
+    "natrix_render_density": [_vp, _i, _i, ctypes.c_int64, _vp, _vp, ctypes.c_int64, _vp],
+    "natrix_quiver_tiles": [_i, _i, _f, ctypes.POINTER(ctypes.c_int32),
+                            ctypes.POINTER(ctypes.c_int32)],
+    "natrix_quiver": [_vp, _i, _i, ctypes.c_int64, _i, _i, _f, _vp, _vp, ctypes.c_int64, _vp],
     "natrix_last_error": [],
     "natrix_version": [],
 }

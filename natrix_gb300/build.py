@@ -30,6 +30,7 @@ UNITS = {
     "noalloc.cu": ["-fmad=false"],
     "particles.cu": ["-fmad=false"],
     "batch.cu": ["-fmad=false"],
+    "render.cu": ["-fmad=false"],
     "unet_conv.cu": [],
     "unet_kernels.cu": [],
 }

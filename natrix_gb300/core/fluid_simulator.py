@@ -282,6 +282,19 @@ class FluidSimulator:
         den = max(sbb - sb * sb / n, 0.0)
         return float(np.sqrt(num / den)) if den > 0 else 0.0
 
+    def residual_regions(self, labels: torch.Tensor, n_labels: int) -> float:
+        """Relative residual with the mean removed per connected fluid region
+        (``labels``: int32 CUDA tensor H x W, region id per fluid cell, < 0 on
+        obstacles; ``warmstart.Regions`` builds them)."""
+        sums = torch.empty(n_labels, 5, dtype=torch.float64, device="cuda")
+        call("natrix_residual_regions", self.handle, ctypes.c_void_p(labels.data_ptr()),
+             int(n_labels), ctypes.c_void_p(sums.data_ptr()), _stream())
+        s = sums.cpu().numpy()
+        n = np.maximum(s[:, 0], 1.0)
+        num = np.maximum(s[:, 2] - s[:, 1] ** 2 / n, 0.0).sum()
+        den = np.maximum(s[:, 4] - s[:, 3] ** 2 / n, 0.0).sum()
+        return float(np.sqrt(num / den)) if den > 0 else 0.0
+
     def jacobi(self, sweeps: int) -> None:
         """Run more Jacobi sweeps on the current pressure (no reset)."""
         self._sync_params()
@@ -299,3 +312,4 @@ class FluidSimulator:
 
 def version() -> str:
     return load().natrix_version().decode()
+

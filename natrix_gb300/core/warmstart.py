@@ -149,6 +149,11 @@ class UNet:
         self.mhw, self.vhw = torch.zeros_like(self.hw), torch.zeros_like(self.hw)
         self.mhb, self.vhb = torch.zeros_like(self.hb), torch.zeros_like(self.hb)
         self.status = torch.zeros(1, dtype=torch.int32, device=device)
+        # fixed output multiplier: p = out_scale * (hw . d1 + hb), set from the
+        # RMS of the training targets so the head's weights stay O(1)
+        self.out_scale = 1.0
+        self._ghw_eff = torch.zeros_like(self.hw)
+        self._ghb_eff = torch.zeros_like(self.hb)
         self.step_count = 0
         self.repack()
         self.acts: dict[str, torch.Tensor] = {}
@@ -173,6 +178,7 @@ class UNet:
         d = {f"{L.name}.w": L.w.cpu() for L in self.layers}
         d.update({f"{L.name}.b": L.b.cpu() for L in self.layers})
         d["head.w"], d["head.b"] = self.hw.cpu(), self.hb.cpu()
+        d["out_scale"] = torch.tensor(self.out_scale)
         return d
 
     def load_state_dict(self, d: dict) -> None:
@@ -181,6 +187,7 @@ class UNet:
             L.b.copy_(d[f"{L.name}.b"])
         self.hw.copy_(d["head.w"])
         self.hb.copy_(d["head.b"])
+        self.out_scale = float(d.get("out_scale", torch.tensor(1.0)))
         self.repack()
 
     def zero_grad(self):
@@ -243,7 +250,10 @@ class UNet:
         c.gate = _p(gate)
         c.out0, c.n0, c.out1 = _p(out0), n0, _p(out1)
         if head_out is not None:
-            c.head_w, c.head_b, c.head_out = _p(self.hw), float(self.hb.item()), _p(head_out)
+            self._hw_eff = self.hw * self.out_scale
+            c.head_w = _p(self._hw_eff)
+            c.head_b = float(self.hb.item()) * self.out_scale
+            c.head_out = _p(head_out)
         c.status = _p(self.status)
         _call("natrix_nn_conv3x3", ctypes.byref(c), _s())
 
@@ -287,8 +297,12 @@ class UNet:
         wg = lambda lay, dz, x0, x1, h, w: _call(  # noqa: E731
             "natrix_nn_wgrad", _p(dz), lay.cout, _p(x0), lay.c0, _p(x1),
             lay.c1 if x1 is not None else 0, B, h, w, _p(lay.gw), _p(lay.gb), _s())
-        _call("natrix_nn_head_back", _p(dp), _p(a["d1"]), 16, n, _p(self.hw), _p(self.ghw),
-              _p(self.ghb), _p(a["g16"]), _s())
+        self._ghw_eff.zero_()
+        self._ghb_eff.zero_()
+        _call("natrix_nn_head_back", _p(dp), _p(a["d1"]), 16, n, _p(self._hw_eff),
+              _p(self._ghw_eff), _p(self._ghb_eff), _p(a["g16"]), _s())
+        self.ghw += self._ghw_eff * self.out_scale
+        self.ghb += self._ghb_eff * self.out_scale
         # c52: dz52 = g16
         wg(L["c52"], a["g16"], a["a51"], None, H, W)
         self._conv(L["c52"], a["g16"], None, B, H, W, a["h16"], gate=a["a51"], backward=True)
@@ -360,6 +374,23 @@ class UNet:
         return loss
 
 
+# ------------------------------------------------------------- cost model
+def forward_cost(B: int, H: int, W: int) -> tuple:
+    """(tensor-core FLOPs, algorithmic HBM bytes) of one ``UNet.forward`` on
+    B images of H x W: every kernel reads its inputs once and writes its
+    outputs once (bf16 activations, 2 bytes per channel).  Per full-resolution
+    pixel: prep 21, c11 48, c12 64, pool 40, c21 24, c22 32, pool 20, c31 12,
+    c32 16, up 40, c41 64, c42 32, up 80, c51 128, c52 + head 68: 689 bytes.
+    FLOPs count the padded K the tensor cores execute (input channels rounded
+    up to 16)."""
+    p1 = B * H * W
+    flops = 0.0
+    for name, c0, c1, cout in LAYERS:
+        level = {"c1": 1, "c2": 2, "c3": 4, "c4": 2, "c5": 1}[name[:2]]
+        flops += 2.0 * (p1 // (level * level)) * 9 * _r16(c0 + c1) * cout
+    return flops, 689.0 * p1
+
+
 # ------------------------------------------------------------------ targets
 def inv_scale_of(div: torch.Tensor, mask: Optional[torch.Tensor]) -> torch.Tensor:
     """1 / RMS of the divergence over fluid cells, per image (B x H x pitch)."""
@@ -372,20 +403,69 @@ def inv_scale_of(div: torch.Tensor, mask: Optional[torch.Tensor]) -> torch.Tenso
     return (1.0 / ms.clamp(min=1e-30).sqrt()).float()
 
 
+class Regions:
+    """Connected fluid regions (4-connected, the stencil's neighbours) of B
+    obstacle masks, numbered across the batch: ``labels`` int64 B x H x W
+    (-1 on obstacle cells), ``n`` regions, ``count`` cells per region.  The
+    pressure operator restricted to fluid cells is pure Neumann on every
+    region (obstacle neighbours and walls mirror the centre), so its null
+    space is one constant per region and a right-hand side is solvable only
+    with each region's mean removed."""
+
+    def __init__(self, mask: Optional[torch.Tensor], B: int, H: int, W: int, device="cuda"):
+        from scipy import ndimage
+
+        if mask is None:
+            lab = np.broadcast_to(np.arange(B, dtype=np.int64).reshape(B, 1, 1), (B, H, W))
+            n = B
+        else:
+            m = mask[:, :, :W].cpu().numpy()
+            lab = np.empty((B, H, W), np.int64)
+            n = 0
+            for b in range(B):
+                l, k = ndimage.label(m[b] == 0)
+                lab[b] = np.where(l > 0, l.astype(np.int64) - 1 + n, -1)
+                n += k
+        self.n = max(n, 1)
+        self.labels = torch.from_numpy(np.ascontiguousarray(lab)).to(device)
+        self.fluid = self.labels >= 0
+        self._idx = self.labels.clamp(min=0).view(-1)
+        ones = self.fluid.double().view(-1)
+        self.count = torch.zeros(self.n, dtype=torch.float64, device=device).index_add_(
+            0, self._idx, ones)
+
+    def project(self, v: torch.Tensor) -> torch.Tensor:
+        """v (B x H x W, float64) with each region's mean removed; 0 on obstacles."""
+        f = self.fluid.view(-1)
+        flat = torch.where(f, v.reshape(-1), torch.zeros((), dtype=v.dtype, device=v.device))
+        sums = torch.zeros(self.n, dtype=v.dtype, device=v.device).index_add_(0, self._idx, flat)
+        mean = sums / self.count.clamp(min=1)
+        return torch.where(f, flat - mean[self._idx], torch.zeros_like(flat)).view_as(v)
+
+    def image_labels(self, b: int) -> tuple:
+        """Labels of image b renumbered from 0 (int32, for natrix_residual_regions)."""
+        lab = self.labels[b]
+        lo = int(lab[lab >= 0].min().item()) if bool((lab >= 0).any()) else 0
+        hi = int(lab.max().item())
+        out = torch.where(lab >= 0, lab - lo, torch.full_like(lab, -1)).to(torch.int32)
+        return out.contiguous(), max(hi - lo + 1, 1)
+
+
 def cg_solve(div: torch.Tensor, mask: Optional[torch.Tensor], inv_scale: torch.Tensor, H: int,
-             W: int, pitch: int, rtol: float = 1e-6, max_iter: int = 20000, check: int = 25):
+             W: int, pitch: int, rtol: float = 1e-6, max_iter: int = 20000, check: int = 25,
+             regions: Optional[Regions] = None):
     """FP64 conjugate gradients for A p = div * inv_scale on the fluid cells
-    of B images (A = the sweep's operator; solution mean-free over fluid
-    cells).  Returns (p float32 B x H x W, relative residuals B, iterations)."""
+    of B images (A = the sweep's operator, symmetric negative semidefinite on
+    the fluid cells).  The right-hand side is projected onto the range of A
+    (each connected fluid region's mean removed), so CG converges; the
+    solution is mean-free per region.  Returns (p float32 B x H x W,
+    relative residuals B, iterations)."""
     B = inv_scale.numel()
     dev = div.device
+    if regions is None:
+        regions = Regions(mask, B, H, W, dev)
     dense = div[:, :, :W].double() * inv_scale.double().view(B, 1, 1)
-    m = mask[:, :, :W] if mask is not None else None
-    fluid = (m == 0).double() if m is not None else torch.ones_like(dense)
-    c = -dense * fluid
-    nf = fluid.sum(dim=(1, 2)).clamp(min=1)
-    c = (c - (c.sum(dim=(1, 2)) / nf).view(B, 1, 1)) * fluid
-    c = c.contiguous()
+    c = regions.project(-dense).contiguous()
     x = torch.zeros_like(c)
     r = c.clone()
     d = r.clone()
@@ -413,11 +493,11 @@ def cg_solve(div: torch.Tensor, mask: Optional[torch.Tensor], inv_scale: torch.T
             rel = (rr / cc.clamp(min=1e-300)).sqrt().cpu()
             if float(rel.max()) <= rtol:
                 break
-    # true relative residual with mean removal, from the final iterate
+    # true relative residual (per-region mean removed), from the final iterate
     _call("natrix_nn_cg_apply", _p(x), mp, B, H, W, pitch, _p(q), _s())
-    res = (c - q) * fluid
-    res = res - (res.sum(dim=(1, 2)) / nf).view(B, 1, 1) * fluid
+    res = regions.project(c - q)
     true_rel = (res.pow(2).sum(dim=(1, 2)) / cc.clamp(min=1e-300)).sqrt().cpu()
+    x = regions.project(x)
     return x.float(), true_rel, it
 
 
@@ -493,20 +573,33 @@ def make_pairs(size: int, n: int, seed: int, rtol: float = 1e-6, batch: int = 64
 
 
 def warm_start_solve(sim, net: Optional[UNet], mask: Optional[torch.Tensor], rtol: float = 1e-4,
-                     check: int = 100, max_sweeps: int = 2_000_000, fallback_sweeps: int = 10,
-                     time_limit_s: float = 120.0) -> dict:
+                     check: int = 100, max_sweeps: int = 200_000_000, fallback_sweeps: int = 10,
+                     time_limit_s: float = 120.0, regions: Optional[Regions] = None) -> dict:
     """Solve the pressure system of the simulator's last step to relative
     residual `rtol` with Jacobi sweeps, from zero (net None) or from the
     network's prediction.  Fallback rule: if the residual after
     `fallback_sweeps` sweeps from the prediction exceeds the residual after
-    as many sweeps from zero, restart from zero.  Returns sweeps, seconds,
-    the residual reached and whether the fallback fired."""
+    as many sweeps from zero, restart from zero.  The residual is taken over
+    the fluid cells of `mask` (the obstacles the step used) with each
+    connected region's mean removed; obstacle cells, whose rows the sweep
+    updates but no fluid cell reads, are left out.  Labelling the regions
+    happens before the clock starts.  Returns sweeps, seconds, the residual
+    reached and whether the fallback fired."""
     import time
 
     from .. import _lib as L
 
     H, W = sim.height, sim.width
     pitch = sim.divergence.stride(0)
+    # residual over the fluid cells of the step's obstacle mask, with each
+    # connected region's mean removed (the operator's null space)
+    if regions is None:
+        regions = Regions(mask.view(1, H, -1) if mask is not None else None, 1, H, W)
+    labels, n_labels = regions.image_labels(0)
+
+    def resid() -> float:
+        return sim.residual_regions(labels, n_labels)
+
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     used_fallback = False
@@ -531,10 +624,10 @@ def warm_start_solve(sim, net: Optional[UNet], mask: Optional[torch.Tensor], rto
         guess = (p[0] / inv[0]).contiguous()
         set_pressure(guess)
         sim.jacobi(fallback_sweeps)
-        r_net = sim.residual()
+        r_net = resid()
         set_pressure(None)
         sim.jacobi(fallback_sweeps)
-        r_zero = sim.residual()
+        r_zero = resid()
         if r_net <= r_zero:
             set_pressure(guess)
             sim.jacobi(fallback_sweeps)
@@ -544,11 +637,54 @@ def warm_start_solve(sim, net: Optional[UNet], mask: Optional[torch.Tensor], rto
     else:
         set_pressure(None)
         sweeps = 0
-    res = sim.residual()
+    res = resid()
     while res > rtol and sweeps < max_sweeps and time.perf_counter() - t0 < time_limit_s:
-        sim.jacobi(check)
-        sweeps += check
-        res = sim.residual()
+        # residual checks every `check` sweeps, then every 5% of the sweeps so far
+        k = max(check, sweeps // 20)
+        sim.jacobi(k)
+        sweeps += k
+        res = resid()
     torch.cuda.synchronize()
     return {"sweeps": sweeps, "seconds": time.perf_counter() - t0, "residual": res,
             "fallback": used_fallback, "converged": res <= rtol}
+
+
+def train(net: UNet, pairs: PairSet, steps: int, batch: int = 64, lr: float = 1e-3,
+          lam: float = 1.0, seed: int = 0, log_every: int = 0) -> list:
+    """Adam on random mini-batches of `pairs` (sampled with replacement)."""
+    size_h, size_w = pairs.target.shape[1], pairs.target.shape[2]
+    P = pairs.div.shape[2]
+    if net.step_count == 0:
+        net.out_scale = float(pairs.target.double().pow(2).mean().sqrt().clamp(min=1e-6))
+    g = torch.Generator().manual_seed(seed)
+    losses = []
+    for it in range(steps):
+        idx = torch.randint(0, pairs.n, (min(batch, pairs.n),), generator=g).cuda()
+        losses.append(net.train_step(pairs.div[idx].contiguous(), pairs.mask[idx].contiguous(),
+                                     pairs.inv_scale[idx].contiguous(),
+                                     pairs.target[idx].contiguous(), size_h, size_w, P, lr=lr,
+                                     lam=lam))
+        if log_every and it % log_every == 0:
+            print(f"step {it} loss {losses[-1]:.5g}", flush=True)
+    net.check_status()
+    return losses
+
+
+def evaluation_system(size: int, seed: int, steps: int = 5):
+    """A simulator of the given size after `steps` steps of the large
+    workload's settings, and the obstacle mask its last step used."""
+    from .. import workloads as wl
+    from .fluid_simulator import FluidSimulator
+
+    sim = FluidSimulator(size, size)
+    sim.iterations, sim.vorticity, sim.viscosity, sim.speed, sim.dissipation = 80, 0.35, 0.0, 5.0, 0.99
+    rng = np.random.default_rng(seed)
+    obst = wl.circle_obstacles(rng, 12, size, size)
+    mask = None
+    for _ in range(steps):
+        for o in obst:
+            sim.add_circle_obstacle((float(o[0]), float(o[1])), float(o[2]))
+        mask = sim.obstacles.clone()
+        sim.add_splats(wl.gauss_splats(rng, 16, size, size, 5.0))
+        sim.update(1 / 60)
+    return sim, mask

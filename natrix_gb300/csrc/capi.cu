@@ -537,6 +537,17 @@ int natrix_residual(natrix_sim* s, double out[5], void* stream) {
     return NATRIX_OK;
 }
 
+int natrix_residual_regions(natrix_sim* s, const int32_t* labels, int32_t n_labels,
+                            double* sums, void* stream) {
+    if (!s || !labels || !sums || n_labels < 1) return fail(NATRIX_EINVAL, "bad arguments");
+    DeviceGuard dg(s->device);
+    cudaStream_t st = stream_of(s, stream);
+    NX_CUDA(launch_residual_labels(s->p[s->p_cur], s->div, s->flags, labels, n_labels, s->g, sums,
+                                   st));
+    s->stats.kernel_launches += 1;
+    return NATRIX_OK;
+}
+
 int natrix_field(natrix_sim* s, int32_t field, void** dev_ptr, int64_t* pitch) {
     if (!s || !dev_ptr || !pitch) return fail(NATRIX_EINVAL, "NULL argument");
     DeviceGuard dg(s->device);

@@ -307,6 +307,16 @@ __global__ void __launch_bounds__(C::THREADS, 1)
         __syncthreads();
         if (!s_ok) return;
 
+        // Side walls on the fast path: the left wall's cell is always this
+        // lane's cell 0 (the region starts HXP = 0 mod 4 columns left of a
+        // tile that starts at a multiple of 4), the right wall's is cell 3
+        // when W = 0 mod 4; the clamped neighbour is the cell itself, so one
+        // lane-uniform select per row replaces the per-cell flag tests and
+        // those wall bits do not make a row slow.
+        const int gx0 = job.tile_x - C::HXP + c0;
+        const bool wall_l = gx0 == 0;
+        const bool wall_r = gx0 + 3 == job.g.W - 1;
+        const uint32_t side = (wall_l ? (uint32_t)NB_L : 0u) | (wall_r ? (uint32_t)NB_R << 24 : 0u);
         float p[R][4], d[R][4];
         uint32_t f[R];
         uint32_t slow = 0;
@@ -318,7 +328,7 @@ __global__ void __launch_bounds__(C::THREADS, 1)
             d[r][0] = b.x; d[r][1] = b.y; d[r][2] = b.z; d[r][3] = b.w;
             f[r] = *reinterpret_cast<const uint32_t*>(Fs + (r0 + r) * C::RXF + c0 +
                                                       (C::HXF - C::HXP));
-            if (__any_sync(FULL, f[r] != 0u)) slow |= 1u << r;
+            if (__any_sync(FULL, (f[r] & ~side) != 0u)) slow |= 1u << r;
         }
         __syncthreads();  // staging consumed: prefetch the next job into it
         if (threadIdx.x == 0 && t + (int)gridDim.x < jobs.n) {
@@ -353,8 +363,10 @@ __global__ void __launch_bounds__(C::THREADS, 1)
                     cur[j] = p[r][j];
                     dn[j] = r < R - 1 ? p[r + 1][j] : below[j];
                 }
-                const float lft = __shfl_up_sync(FULL, cur[3], 1);
-                const float rgt = __shfl_down_sync(FULL, cur[0], 1);
+                float lft = __shfl_up_sync(FULL, cur[3], 1);
+                float rgt = __shfl_down_sync(FULL, cur[0], 1);
+                lft = wall_l ? cur[0] : lft;
+                rgt = wall_r ? cur[3] : rgt;
                 const float L[4] = {lft, cur[0], cur[1], cur[2]};
                 const float Rn[4] = {cur[1], cur[2], cur[3], rgt};
                 if (slow & (1u << r)) {

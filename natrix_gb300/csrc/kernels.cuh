@@ -110,6 +110,12 @@ cudaError_t launch_residual(const float* p, const float* div, const uint8_t* mas
                             const uint8_t* flags, Grid g, const StepParams* sp,
                             double* partials, double* out, cudaStream_t st);
 
+// Per-region residual sums: labels dense W*H (fluid region id, < 0 for
+// obstacles), sums n_labels x 5 doubles (zeroed first).
+cudaError_t launch_residual_labels(const float* p, const float* div, const uint8_t* flags,
+                                   const int* labels, int n_labels, Grid g, double* sums,
+                                   cudaStream_t st);
+
 // ---- Jacobi (jacobi_tma.cu) ------------------------------------------------
 // Jacobi tile kernels: shared-memory sweeps on 64x32 tiles, or register tiled
 // with 112x112 / 112x128 output tiles.

@@ -118,6 +118,54 @@ __global__ void __launch_bounds__(RES_THREADS)
     }
 }
 
+// The same sums per connected fluid region: labels[y*W + x] in [0, n) for
+// fluid cells, < 0 for obstacle cells.  The pressure system is pure Neumann
+// on each region, so its residual is only defined up to each region's mean.
+// Warps whose lanes share one label (the common case) reduce first and add
+// once; mixed warps add per lane.
+__global__ void __launch_bounds__(RES_THREADS)
+    k_residual_labels(const float* __restrict__ p, const float* __restrict__ div,
+                      const uint8_t* __restrict__ flags, const int* __restrict__ labels, Grid g,
+                      double* __restrict__ sums) {
+    const long total = (long)g.W * g.H;
+    const long lin = (long)blockIdx.x * RES_THREADS + threadIdx.x;
+    int lab = -1;
+    double v[5] = {0, 0, 0, 0, 0};
+    if (lin < total) {
+        const int y = (int)(lin / g.W), x = (int)(lin % g.W);
+        lab = labels[lin];
+        if (lab >= 0) {
+            const Nbr n = nbrs(g, x, y);
+            const uint8_t f = flags[n.c];
+            const double pc = p[n.c];
+            const double x1 = (f & NB_L) ? pc : (double)p[n.l];
+            const double x2 = (f & NB_R) ? pc : (double)p[n.r];
+            const double y1 = (f & NB_B) ? pc : (double)p[n.b];
+            const double y2 = (f & NB_T) ? pc : (double)p[n.t];
+            const double b = div[n.c];
+            const double r = b - ((x1 + x2 + y1 + y2) - 4.0 * pc);
+            v[0] = 1.0;
+            v[1] = r;
+            v[2] = r * r;
+            v[3] = b;
+            v[4] = b * b;
+        }
+    }
+    const int l0 = __shfl_sync(0xffffffffu, lab, 0);
+    const bool uniform = __all_sync(0xffffffffu, lab == l0);
+    if (uniform) {
+        if (l0 < 0) return;
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            const double t = warp_sum(v[j]);
+            if ((threadIdx.x & 31) == 0) atomicAdd(sums + (size_t)l0 * 5 + j, t);
+        }
+    } else if (lab >= 0) {
+#pragma unroll
+        for (int j = 0; j < 5; ++j) atomicAdd(sums + (size_t)lab * 5 + j, v[j]);
+    }
+}
+
 __global__ void k_residual_final(const double* __restrict__ partials, int nblocks,
                                  double* __restrict__ out) {
     __shared__ double s[32][5];
@@ -135,6 +183,17 @@ __global__ void k_residual_final(const double* __restrict__ partials, int nblock
 }
 
 }  // namespace
+
+cudaError_t launch_residual_labels(const float* p, const float* div, const uint8_t* flags,
+                                   const int* labels, int n_labels, Grid g, double* sums,
+                                   cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(sums, 0, (size_t)n_labels * 5 * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    const long total = (long)g.W * g.H;
+    k_residual_labels<<<(unsigned)((total + RES_THREADS - 1) / RES_THREADS), RES_THREADS, 0, st>>>(
+        p, div, flags, labels, g, sums);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_obstacles(uint8_t* mask, Grid g, const ShapeOp* ops, int n, int fresh,
                              cudaStream_t st) {

@@ -7,24 +7,29 @@
 //     X[pixel + offset(t), c] * Wp[n, t, c]
 // M = 128 pixels of one image row, N = output channels, K = 9 * C.
 //
-// One persistent CTA per SM, six warps:
-//   warp 0 lane 0  TMA producer: per tap, one 4-D box {8 channels, 128 px}
-//                  per 8-channel chunk (out-of-image pixels and channels read
-//                  as zero, which is the padding), into a 4-stage ring;
-//   warp 1 lane 0  MMA issuer: per tap, C/16 tcgen05.mma (K = 16 each) into
-//                  one of two TMEM accumulators; tcgen05.commit releases the
-//                  ring stage and, after the last tap, hands the accumulator
-//                  to the epilogue;
+// One persistent CTA per SM, six warps, walking "segments": S consecutive
+// output rows of one 128-pixel column strip of one image.  A segment's S + 2
+// input rows stream through a ring of R row stages, each input row loaded
+// once and used by the three output rows it touches; the three horizontal
+// taps of a row read the same stage at byte offsets 0, 16 and 32 (one pixel
+// = 16 bytes of an 8-channel chunk, SWIZZLE_NONE rows are 16-byte granular).
+//   warp 0 lane 0  TMA producer: per input row, one 4-D box {8 channels,
+//                  136 px from x0 - 1} per 8-channel chunk (out-of-image
+//                  pixels and channels read as zero, which is the padding);
+//   warp 1 lane 0  MMA issuer: per output row, 9 taps x C/16 tcgen05.mma
+//                  (K = 16 each) into one of two TMEM accumulators;
+//                  tcgen05.commit hands the accumulator to the epilogue and
+//                  frees the input row no later output row reads;
 //   warps 2-5      epilogue: tcgen05.ld of their 32-lane quarter, bias, ReLU
 //                  or ReLU-gate, optional 1x1 head, bf16 NHWC stores.
 // The weights (packed once per layer in the operand layout) are copied to
 // shared memory once per CTA with cp.async.bulk.
 //
 // Operand layout (validated SWIZZLE_NONE K-major, see umma.cuh): a TMA box of
-// 8 channels x 128 pixels lands as 16 consecutive 8x16-byte core matrices,
-// so chunk q of a stage starts at q * 2048 bytes: LBO = 2048, SBO = 128.  The
-// packed weights use LBO = N/8 * 128, SBO = 128 with K chunks ordered
-// (tap, channel chunk).
+// 8 channels x 136 pixels lands as 136 consecutive 16-byte rows, so chunk q of
+// a stage starts at q * 2176 bytes: LBO = 2176, SBO = 128.  The packed
+// weights use LBO = N/8 * 128, SBO = 128 with K chunks ordered (tap, channel
+// chunk).
 //
 // Every wait is bounded; a role that gives up records status bit 2 and
 // leaves its loop, the others then time out too, and the allocating warp
@@ -42,9 +47,10 @@ namespace natrix {
 
 namespace {
 
-constexpr int kStages = 4;
+constexpr int kMaxStages = 32;
 constexpr int kTileM = 128;
-constexpr int kChunkBytes = 8 * kTileM * 2;  // one 8-channel box: 2048 B
+constexpr int kBoxW = 136;                   // pixels per box: x0 - 1 .. x0 + 128, padded
+constexpr int kChunkBytes = 8 * kBoxW * 2;   // one 8-channel box: 2176 B
 
 struct ConvParams {
     int B, H, W;
@@ -62,10 +68,29 @@ struct ConvParams {
     float head_b;
     float* head_out;        // B*H*W floats, or null
     int* status;
-    int tiles_x, n_tiles;
+    int tiles_x;            // 128-pixel column strips per row
+    int seg_rows, n_segs;   // output rows per segment, segments per strip
+    int n_units;            // B * tiles_x * n_segs
+    int stages;             // input-row ring depth (3 .. kMaxStages)
+    uint32_t stage_bytes;
     uint32_t smem_w, smem_a;  // byte offsets in dynamic shared memory
     uint32_t tmem_cols;
 };
+
+struct Unit {
+    int b, tx, y0, rows;
+};
+
+__device__ __forceinline__ Unit unit_of(const ConvParams& P, int u) {
+    Unit r;
+    r.tx = u % P.tiles_x;
+    const int rest = u / P.tiles_x;
+    const int seg = rest % P.n_segs;
+    r.b = rest / P.n_segs;
+    r.y0 = seg * P.seg_rows;
+    r.rows = min(P.seg_rows, P.H - r.y0);
+    return r;
+}
 
 __device__ __forceinline__ float bf16_to_f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
 
@@ -80,15 +105,16 @@ __global__ void __launch_bounds__(192, 1)
     k_conv3x3_tc(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
                  const ConvParams P) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2], wbar;
+    __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], wbar;
     __shared__ uint32_t tmem_slot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int chunks = P.ctot / 8;  // 8-channel chunks per tap
+    const int chunks = P.ctot / 8;  // 8-channel chunks per input row
     const int c0_chunks = P.c0 / 8;
     const int c1_chunks = P.c1 / 8;
+    const uint32_t R = (uint32_t)P.stages;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < P.stages; ++s) {
             umma::mbar_init(&full[s], 1);
             umma::mbar_init(&empty[s], 1);
         }
@@ -107,39 +133,34 @@ __global__ void __launch_bounds__(192, 1)
     const uint32_t wbytes = (uint32_t)P.N * 9u * (uint32_t)P.ctot * 2u;
 
     if (warp == 0 && lane == 0) {
-        // weights once, then the activation ring
+        // weights once, then the input rows of every segment through the ring
         umma::mbar_arrive_expect_tx(&wbar, wbytes);
         for (uint32_t off = 0; off < wbytes; off += 32768u) {
             const uint32_t n = wbytes - off < 32768u ? wbytes - off : 32768u;
             umma::bulk_load(smem + P.smem_w + off, reinterpret_cast<const unsigned char*>(P.wpack) + off,
                             n, &wbar);
         }
-        int s = 0;
-        uint32_t phase = 0;
+        uint32_t g = 0;  // input rows loaded so far
         bool ok = true;
-        for (int tile = blockIdx.x; tile < P.n_tiles && ok; tile += gridDim.x) {
-            const int tx = tile % P.tiles_x, rest = tile / P.tiles_x;
-            const int y = rest % P.H, b = rest / P.H;
-            const int x0 = tx * kTileM;
-            for (int t = 0; t < 9 && ok; ++t) {
-                const int dy = t / 3 - 1, dx = t % 3 - 1;
-                if (!umma::mbar_wait(&empty[s], phase ^ 1u)) {
+        for (int u = blockIdx.x; u < P.n_units && ok; u += gridDim.x) {
+            const Unit U = unit_of(P, u);
+            const int x0 = U.tx * kTileM;
+            for (int k = 0; k < U.rows + 2; ++k, ++g) {
+                const uint32_t s = g % R;
+                if (!umma::mbar_wait(&empty[s], ((g / R) & 1u) ^ 1u)) {
                     ok = false;
                     break;
                 }
                 umma::mbar_arrive_expect_tx(&full[s], (uint32_t)chunks * kChunkBytes);
-                unsigned char* dst = smem + P.smem_a + (uint32_t)s * chunks * kChunkBytes;
+                unsigned char* dst = smem + P.smem_a + s * P.stage_bytes;
+                const int y = U.y0 - 1 + k;
                 for (int q = 0; q < chunks; ++q) {
                     if (q < c0_chunks || c1_chunks == 0)
-                        umma::tma_load_4d(dst + q * kChunkBytes, &tm0, 8 * q, x0 + dx, y + dy, b,
+                        umma::tma_load_4d(dst + q * kChunkBytes, &tm0, 8 * q, x0 - 1, y, U.b,
                                           &full[s]);
                     else
-                        umma::tma_load_4d(dst + q * kChunkBytes, &tm1, 8 * (q - c0_chunks), x0 + dx,
-                                          y + dy, b, &full[s]);
-                }
-                if (++s == kStages) {
-                    s = 0;
-                    phase ^= 1u;
+                        umma::tma_load_4d(dst + q * kChunkBytes, &tm1, 8 * (q - c0_chunks), x0 - 1,
+                                          y, U.b, &full[s]);
                 }
             }
         }
@@ -150,39 +171,47 @@ __global__ void __launch_bounds__(192, 1)
         const uint32_t lbo_b = (uint32_t)(P.N / 8) * 128u;
         const uint32_t w0 = umma::smem_u32(smem + P.smem_w);
         const uint32_t a0 = umma::smem_u32(smem + P.smem_a);
-        int s = 0, acc = 0;
-        uint32_t phase = 0, acc_phase = 0;
-        for (int tile = blockIdx.x; tile < P.n_tiles && ok; tile += gridDim.x) {
-            if (!umma::mbar_wait(&acc_empty[acc], acc_phase ^ 1u)) {
-                ok = false;
-                break;
-            }
-            umma::fence_after_sync();
-            const uint32_t d = tmem + (uint32_t)(acc * P.N);
-            for (int t = 0; t < 9 && ok; ++t) {
-                if (!umma::mbar_wait(&full[s], phase)) {
+        uint32_t g = 0;  // first input row of the current segment
+        int acc = 0;
+        uint32_t acc_phase = 0;
+        for (int u = blockIdx.x; u < P.n_units && ok; u += gridDim.x) {
+            const Unit U = unit_of(P, u);
+            for (int i = 0; i < U.rows && ok; ++i) {
+                if (!umma::mbar_wait(&acc_empty[acc], acc_phase ^ 1u)) {
                     ok = false;
                     break;
                 }
+                uint32_t sa[3];
+                for (int dy = 0; dy < 3 && ok; ++dy) {
+                    const uint32_t row = g + (uint32_t)(i + dy);
+                    sa[dy] = a0 + (row % R) * P.stage_bytes;
+                    ok = umma::mbar_wait(&full[row % R], (row / R) & 1u);
+                }
+                if (!ok) break;
                 umma::fence_after_sync();
-                const uint32_t sa = a0 + (uint32_t)s * chunks * kChunkBytes;
-                for (int m = 0; m < chunks / 2; ++m) {
-                    const uint64_t ad = umma::smem_desc(sa + 2u * m * kChunkBytes, kChunkBytes, 128);
-                    const uint64_t bd =
-                        umma::smem_desc(w0 + (uint32_t)(t * chunks + 2 * m) * lbo_b, lbo_b, 128);
-                    umma::mma_bf16(d, ad, bd, idesc, (t > 0 || m > 0) ? 1u : 0u);
+                const uint32_t d = tmem + (uint32_t)(acc * P.N);
+                for (int t = 0; t < 9; ++t) {
+                    const int dy = t / 3, dx = t % 3;
+                    for (int m = 0; m < chunks / 2; ++m) {
+                        const uint64_t ad = umma::smem_desc(
+                            sa[dy] + (uint32_t)dx * 16u + 2u * m * kChunkBytes, kChunkBytes, 128);
+                        const uint64_t bd =
+                            umma::smem_desc(w0 + (uint32_t)(t * chunks + 2 * m) * lbo_b, lbo_b, 128);
+                        umma::mma_bf16(d, ad, bd, idesc, (t > 0 || m > 0) ? 1u : 0u);
+                    }
                 }
-                umma::commit(&empty[s]);
-                if (++s == kStages) {
-                    s = 0;
-                    phase ^= 1u;
+                umma::commit(&acc_full[acc]);
+                // input row i has no later reader in this segment
+                umma::commit(&empty[(g + (uint32_t)i) % R]);
+                if (++acc == 2) {
+                    acc = 0;
+                    acc_phase ^= 1u;
                 }
             }
-            umma::commit(&acc_full[acc]);
-            if (++acc == 2) {
-                acc = 0;
-                acc_phase ^= 1u;
-            }
+            if (!ok) break;
+            umma::commit(&empty[(g + (uint32_t)U.rows) % R]);
+            umma::commit(&empty[(g + (uint32_t)U.rows + 1u) % R]);
+            g += (uint32_t)U.rows + 2u;
         }
         if (!ok) atomicOr(P.status, 2);
     } else if (warp >= 2) {
@@ -190,70 +219,74 @@ __global__ void __launch_bounds__(192, 1)
         const int row = quarter * 32 + lane;
         int acc = 0;
         uint32_t acc_phase = 0;
-        for (int tile = blockIdx.x; tile < P.n_tiles; tile += gridDim.x) {
-            bool ok = true;
-            if (lane == 0) ok = umma::mbar_wait(&acc_full[acc], acc_phase);
-            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-            if (!ok) {
-                if (lane == 0) atomicOr(P.status, 2);
-                break;
-            }
-            umma::fence_after_sync();
-            const int tx = tile % P.tiles_x, rest = tile / P.tiles_x;
-            const int y = rest % P.H, b = rest / P.H;
-            const int x = tx * kTileM + row;
+        bool ok = true;
+        for (int u = blockIdx.x; u < P.n_units && ok; u += gridDim.x) {
+            const Unit U = unit_of(P, u);
+            const int x = U.tx * kTileM + row;
             const bool inside = x < P.W;
-            const size_t pix = ((size_t)b * P.H + y) * P.W + (inside ? x : 0);
-            float head = P.head_b;
-            for (int c = 0; c < P.N; c += 16) {
-                float v[16];
-                umma::tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * P.N + c), v);
-                if (!inside) continue;
-                if (P.bias)
+            for (int i = 0; i < U.rows; ++i) {
+                if (lane == 0) ok = umma::mbar_wait(&acc_full[acc], acc_phase);
+                ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+                if (!ok) {
+                    if (lane == 0) atomicOr(P.status, 2);
+                    break;
+                }
+                umma::fence_after_sync();
+                const int y = U.y0 + i;
+                const size_t pix = ((size_t)U.b * P.H + y) * P.W + (inside ? x : 0);
+                float head = P.head_b;
+                for (int c = 0; c < P.N; c += 16) {
+                    float v[16];
+                    umma::tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * P.N + c),
+                                    v);
+                    if (!inside) continue;
+                    if (P.bias)
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) v[j] += P.bias[c + j];
-                if (P.relu)
+                        for (int j = 0; j < 16; ++j) v[j] += P.bias[c + j];
+                    if (P.relu)
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) v[j] = v[j] > 0.0f ? v[j] : 0.0f;
-                if (P.gate) {
-                    const uint4* g = reinterpret_cast<const uint4*>(P.gate + pix * P.N + c);
-                    const uint4 g0 = g[0], g1 = g[1];
-                    const uint32_t gw[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+                        for (int j = 0; j < 16; ++j) v[j] = v[j] > 0.0f ? v[j] : 0.0f;
+                    if (P.gate) {
+                        const uint4* gp = reinterpret_cast<const uint4*>(P.gate + pix * P.N + c);
+                        const uint4 g0 = gp[0], g1 = gp[1];
+                        const uint32_t gw[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        const uint16_t h = (uint16_t)(gw[j / 2] >> (16 * (j & 1)));
-                        if (!(bf16_to_f(h) > 0.0f)) v[j] = 0.0f;
+                        for (int j = 0; j < 16; ++j) {
+                            const uint16_t h = (uint16_t)(gw[j / 2] >> (16 * (j & 1)));
+                            if (!(bf16_to_f(h) > 0.0f)) v[j] = 0.0f;
+                        }
+                    }
+                    if (P.head_out)
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) head += P.head_w[c + j] * v[j];
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        packed[j] =
+                            (uint32_t)f_to_bf16(v[2 * j]) | ((uint32_t)f_to_bf16(v[2 * j + 1]) << 16);
+                    uint16_t* dst = nullptr;
+                    size_t off = 0;
+                    if (c < P.n0 && P.out0) {
+                        dst = P.out0;
+                        off = pix * P.n0 + c;
+                    } else if (c >= P.n0 && P.out1) {
+                        dst = P.out1;
+                        off = pix * (P.N - P.n0) + (c - P.n0);
+                    }
+                    if (dst) {
+                        uint4* o = reinterpret_cast<uint4*>(dst + off);
+                        o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                        o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
                     }
                 }
-                if (P.head_out)
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) head += P.head_w[c + j] * v[j];
-                uint32_t packed[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j)
-                    packed[j] = (uint32_t)f_to_bf16(v[2 * j]) | ((uint32_t)f_to_bf16(v[2 * j + 1]) << 16);
-                uint16_t* dst = nullptr;
-                size_t off = 0;
-                if (c < P.n0 && P.out0) {
-                    dst = P.out0;
-                    off = pix * P.n0 + c;
-                } else if (c >= P.n0 && P.out1) {
-                    dst = P.out1;
-                    off = pix * (P.N - P.n0) + (c - P.n0);
+                if (inside && P.head_out) P.head_out[pix] = head;
+                umma::fence_before_sync();
+                __syncwarp();
+                if (lane == 0) umma::mbar_arrive(&acc_empty[acc]);
+                if (++acc == 2) {
+                    acc = 0;
+                    acc_phase ^= 1u;
                 }
-                if (dst) {
-                    uint4* o = reinterpret_cast<uint4*>(dst + off);
-                    o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                    o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-                }
-            }
-            if (inside && P.head_out) P.head_out[pix] = head;
-            umma::fence_before_sync();
-            __syncwarp();
-            if (lane == 0) umma::mbar_arrive(&acc_empty[acc]);
-            if (++acc == 2) {
-                acc = 0;
-                acc_phase ^= 1u;
             }
         }
     }
@@ -275,13 +308,13 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 4-D map of an NHWC bf16 tensor with an {8 channels, 128 pixels} box.
+// 4-D map of an NHWC bf16 tensor with an {8 channels, 136 pixels} box.
 bool encode_nhwc(CUtensorMap* map, const void* base, int B, int H, int W, int C) {
     auto fn = encode_fn();
     if (!fn) return false;
     cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
     cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
-    cuuint32_t box[4] = {8, (cuuint32_t)kTileM, 1, 1};
+    cuuint32_t box[4] = {8, (cuuint32_t)kBoxW, 1, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
     return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box,
               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -329,17 +362,31 @@ extern "C" int natrix_nn_conv3x3(const natrix_nn_conv* c, void* stream) {
     P.head_out = c->head_out;
     P.status = c->status;
     P.tiles_x = (c->W + kTileM - 1) / kTileM;
-    P.n_tiles = P.tiles_x * c->H * c->B;
+    const int sms = num_sms_dev();
+    // segments: long enough that the 2 halo rows cost little, short enough
+    // that every SM gets several
+    int S = 64;
+    auto units = [&](int rows) { return (long)c->B * P.tiles_x * ((c->H + rows - 1) / rows); };
+    while (S > 8 && units(S) < 8L * sms) S /= 2;
+    if (S > c->H) S = c->H;
+    P.seg_rows = S;
+    P.n_segs = (c->H + S - 1) / S;
+    if (units(S) > 0x7fffffffL) return set_last_error(NATRIX_EINVAL, "conv: too many segments");
+    P.n_units = (int)units(S);
     const uint32_t wbytes = (uint32_t)P.N * 9u * (uint32_t)P.ctot * 2u;
     P.smem_w = 0;
     P.smem_a = (wbytes + 1023u) / 1024u * 1024u;
-    const uint32_t abytes = (uint32_t)kStages * (P.ctot / 8) * kChunkBytes;
-    const uint32_t smem = P.smem_a + abytes;
+    P.stage_bytes = (uint32_t)(P.ctot / 8) * kChunkBytes;
+    const uint32_t budget = 200u * 1024u;
+    const long room = (long)budget - (long)P.smem_a;
+    const long fit = room > 0 ? room / (long)P.stage_bytes : 0;
+    if (fit < 3)
+        return set_last_error(NATRIX_EINVAL, "conv: weights + three input rows exceed shared memory");
+    P.stages = (int)(fit < kMaxStages ? fit : kMaxStages);
+    const uint32_t smem = P.smem_a + (uint32_t)P.stages * P.stage_bytes;
     uint32_t cols = 32;
     while (cols < 2u * (uint32_t)P.N) cols *= 2;
     P.tmem_cols = cols;
-    if (smem > 200u * 1024u)
-        return set_last_error(NATRIX_EINVAL, "conv: weights + activation ring exceed shared memory");
     if (!P.status) return set_last_error(NATRIX_EINVAL, "conv: status word required");
     CUtensorMap tm0, tm1;
     if (!encode_nhwc(&tm0, c->src0, c->B, c->H, c->W, c->c0) ||
@@ -353,7 +400,7 @@ extern "C" int natrix_nn_conv3x3(const natrix_nn_conv* c, void* stream) {
             return set_last_error(NATRIX_ECUDA, "conv: shared memory attribute");
         attr = true;
     }
-    const int grid = P.n_tiles < num_sms_dev() ? P.n_tiles : num_sms_dev();
+    const int grid = P.n_units < sms ? P.n_units : sms;
     k_conv3x3_tc<<<grid, 192, smem, reinterpret_cast<cudaStream_t>(stream)>>>(tm0, tm1, P);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_last_error(NATRIX_ECUDA, cudaGetErrorString(e));

@@ -5,5 +5,5 @@ here="$(cd "$(dirname "$0")" && pwd)"
 mkdir -p "$here/_build"
 ${CC:-gcc} -std=c11 -O2 -fopenmp -ffp-contract=off -fno-fast-math -fPIC -shared \
     -Wall -Wno-unknown-pragmas \
-    "$here/oracle.c" -o "$here/_build/liboracle.so" -lm
+    "$here/oracle.c" "$here/render.c" -o "$here/_build/liboracle.so" -lm
 echo "built $here/_build/liboracle.so"

@@ -35,8 +35,8 @@ _dblp = ctypes.POINTER(ctypes.c_double)
 
 
 def build(force: bool = False) -> Path:
-    """Compile oracle.c (gcc, OpenMP) if the library is missing or stale."""
-    src = [_HERE / "oracle.c", _HERE / "oracle_impl.h"]
+    """Compile oracle.c and render.c (gcc, OpenMP) if the library is missing or stale."""
+    src = [_HERE / "oracle.c", _HERE / "oracle_impl.h", _HERE / "render.c"]
     if force or not _LIB_PATH.exists() or any(
             s.stat().st_mtime > _LIB_PATH.stat().st_mtime for s in src):
         subprocess.run(["bash", str(_HERE / "build_oracle.sh")], check=True,
@@ -218,6 +218,41 @@ def relative_residual(p, div, obs) -> float:
     return rel_from_sums(residual_sums(p, div, obs))
 
 
+def fluid_labels(obs) -> tuple:
+    """4-connected fluid regions of an obstacle mask: int32 labels (-1 on
+    obstacles) and their number."""
+    from scipy import ndimage
+
+    lab, n = ndimage.label(np.asarray(obs) == 0)
+    return (lab.astype(np.int32) - 1), max(int(n), 1)
+
+
+def residual_sums_regions(p, div, obs, labels, n_labels) -> np.ndarray:
+    """{n, sum r, sum r^2, sum b, sum b^2} per connected fluid region."""
+    H, W = p.shape
+    out = np.zeros((n_labels, 5), np.float64)
+    labels = np.ascontiguousarray(labels, np.int32)
+    getattr(lib(), "orc_residual_regions" + _sfx(p.dtype))(
+        _p(p), _p(div), _p(obs), _p(labels), n_labels, W, H, _p(out))
+    return out
+
+
+def rel_from_region_sums(s) -> float:
+    """sqrt(sum ||r - mean r||^2 / sum ||b - mean b||^2), means per region."""
+    s = np.asarray(s, np.float64).reshape(-1, 5)
+    n = np.maximum(s[:, 0], 1.0)
+    num = np.maximum(s[:, 2] - s[:, 1] ** 2 / n, 0.0).sum()
+    den = np.maximum(s[:, 4] - s[:, 3] ** 2 / n, 0.0).sum()
+    return float(math.sqrt(num / den)) if den > 0 else 0.0
+
+
+def relative_residual_regions(p, div, obs) -> float:
+    """Relative residual over the fluid cells with each connected region's
+    mean removed (the null space of the pure-Neumann system on the fluid)."""
+    labels, n = fluid_labels(obs)
+    return rel_from_region_sums(residual_sums_regions(p, div, np.ascontiguousarray(obs), labels, n))
+
+
 def rel_from_sums(s) -> float:
     n, sr, srr, sb, sbb = (float(x) for x in s)
     if n <= 0:
@@ -351,3 +386,43 @@ class OracleDensity:
             advect_particle(self.buf[self.r], self.buf[self.r ^ 1], self.fluid.velocity,
                             self.fluid.obstacles, dt, self.speed, self.dissipation)
             self.r ^= 1
+
+
+# ---- headless visualisation (oracle/render.c) ----
+def plasma_palette() -> np.ndarray:
+    """(256, 4) uint8: the field shader's colour for each texel byte."""
+    pal = np.empty((256, 4), np.uint8)
+    lib().orc_plasma_palette(_p(pal))
+    return pal
+
+
+def render_density(rho) -> tuple:
+    """float32 (H, W) density -> (texture, colour), each (H, W, 4) uint8."""
+    rho = np.ascontiguousarray(rho, np.float32)
+    H, W = rho.shape
+    tex = np.empty((H, W, 4), np.uint8)
+    col = np.empty((H, W, 4), np.uint8)
+    lib().orc_render_density(_p(rho), W, H, _p(tex), _p(col))
+    return tex, col
+
+
+def quiver_tiles(win_w: int, win_h: int, tile: float) -> tuple:
+    t = np.float32(tile)
+    nx = int(np.floor((np.float32(win_w) - np.float32(0.5)) / t)) + 1
+    ny = int(np.floor((np.float32(win_h) - np.float32(0.5)) / t)) + 1
+    return nx, ny
+
+
+def quiver(v, win_w: int, win_h: int, tile: float, overlay: bool = True) -> tuple:
+    """float32 velocity (H, W, 2) -> (arrows (ny, nx, 2) float32, overlay
+    (win_h, win_w, 4) uint8 or None)."""
+    v = np.ascontiguousarray(v, np.float32)
+    VH, VW = v.shape[:2]
+    nx, ny = quiver_tiles(win_w, win_h, tile)
+    arrows = np.empty((ny, nx, 2), np.float32)
+    lib().orc_quiver_arrows(_p(v), VW, VH, win_w, win_h, ctypes.c_float(tile), _p(arrows), nx, ny)
+    out = None
+    if overlay:
+        out = np.empty((win_h, win_w, 4), np.uint8)
+        lib().orc_quiver_overlay(_p(arrows), nx, win_w, win_h, ctypes.c_float(tile), _p(out))
+    return arrows, out

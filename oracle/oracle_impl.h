@@ -430,6 +430,34 @@ void FN(orc_residual)(const REAL* p, const REAL* div, const unsigned char* obs, 
     out[4] = sbb;
 }
 
+/* The same residual sums per connected fluid region: labels[i] in
+ * [0, n_labels) on fluid cells, < 0 on obstacles; out holds n_labels x 5
+ * doubles (zeroed here).  The system is pure Neumann on each region, so its
+ * residual is defined up to one constant per region. */
+void FN(orc_residual_regions)(const REAL* p, const REAL* div, const unsigned char* obs,
+                              const int* labels, int n_labels, int W, int H, double* out) {
+    for (long k = 0; k < (long)n_labels * 5; ++k) out[k] = 0;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            long L, R, B, T, i = (long)y * W + x;
+            if (obs[i] || labels[i] < 0) continue;
+            FN(nbrs)(x, y, W, H, &L, &R, &B, &T);
+            double pc = p[i];
+            double x1 = obs[L] ? pc : (double)p[L];
+            double x2 = obs[R] ? pc : (double)p[R];
+            double y1 = obs[B] ? pc : (double)p[B];
+            double y2 = obs[T] ? pc : (double)p[T];
+            double b = div[i];
+            double r = b - ((x1 + x2 + y1 + y2) - 4.0 * pc);
+            double* o = out + (long)labels[i] * 5;
+            o[0] += 1;
+            o[1] += r;
+            o[2] += r * r;
+            o[3] += b;
+            o[4] += b * b;
+        }
+}
+
 /* Lagrangian particles (no reference counterpart): RK2 midpoint advection in
  * the velocity field with the AdvectVelocity sampler, positions in cells,
  * displacement = v * dt * speed as in the reference, clamped to the grid:

@@ -5,6 +5,8 @@ against the golden vectors written from the reference's own shaders; within
 the stated tolerance against the float64 oracle."""
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -139,6 +141,8 @@ def test_temporal_blocking_is_bit_identical(cuda, oracle):
 def test_jacobi_sweeps_isolated(cuda, oracle):
     """natrix_jacobi on an uploaded pressure/divergence equals the oracle's
     sweeps with the last step's obstacles, for several sweep counts."""
+    import torch
+
     from natrix_gb300 import _lib
 
     W, H = 123, 77
@@ -163,6 +167,17 @@ def test_jacobi_sweeps_isolated(cuda, oracle):
         rs = sim.residual_sums()
         want = oracle.residual_sums(got, b, mask)
         np.testing.assert_allclose(rs, want, rtol=1e-9, atol=1e-9)
+        # per connected fluid region (the circle and triangle cut off pockets)
+        labels, n = oracle.fluid_labels(mask)
+        want_r = oracle.residual_sums_regions(got, b, mask, labels, n)
+        got_r = torch.empty(n, 5, dtype=torch.float64, device="cuda")
+        _lib.call("natrix_residual_regions", sim.handle,
+                  ctypes.c_void_p(torch.from_numpy(labels).cuda().data_ptr()), n,
+                  ctypes.c_void_p(got_r.data_ptr()), None)
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(got_r.cpu().numpy(), want_r, rtol=1e-9, atol=1e-9)
+        dl = torch.from_numpy(labels).cuda()
+        assert abs(sim.residual_regions(dl, n) - oracle.rel_from_region_sums(want_r)) < 1e-9
     sim.sync()
     den.destroy()
     sim.destroy()

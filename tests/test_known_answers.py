@@ -105,3 +105,27 @@ def test_particles_rk2_uniform_flow(oracle):
     np.testing.assert_array_equal(cells, [[11, 10], [31, 3]])
     rho = oracle.particles_splat(pos, W, H)
     assert abs(rho.sum() - 2.0) < 1e-6
+
+
+def test_region_residual_ignores_per_region_constants(oracle):
+    """A wall of obstacles splits the fluid into two regions; the residual
+    with per-region means removed is blind to a constant added per region to
+    the pressure or the divergence, while the global-mean residual is not
+    (and no sweep can remove that part)."""
+    rng = np.random.default_rng(4)
+    W, H = 20, 16
+    mask = np.zeros((H, W), np.uint8)
+    mask[:, 9] = 1
+    labels, n = oracle.fluid_labels(mask)
+    assert n == 2 and labels[0, 0] != labels[0, 15] and labels[0, 9] == -1
+    p = rng.normal(size=(H, W))
+    b = rng.normal(size=(H, W))
+    base = oracle.relative_residual_regions(p, b, mask)
+    shift = np.where(labels == labels[0, 0], 3.0, -2.0) * (mask == 0)
+    assert abs(oracle.relative_residual_regions(p + shift, b, mask) - base) < 1e-12
+    b2 = b + shift
+    p2 = oracle.jacobi_n(np.zeros((H, W)), b2, mask, 4000)
+    assert oracle.relative_residual_regions(p2, b2, mask) < 1e-6
+    assert oracle.relative_residual(p2, b2, mask) > 1e-2
+    sums = oracle.residual_sums_regions(p, b, mask, labels, n)
+    np.testing.assert_allclose(sums.sum(axis=0), oracle.residual_sums(p, b, mask), rtol=1e-12)
