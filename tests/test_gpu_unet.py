@@ -278,8 +278,18 @@ def test_training_reduces_loss_and_warm_start_gain(cuda, capsys):
         mask = sim.obstacles.clone()
         sim.add_splats(wl.gauss_splats(rng, 16, size, size, 5.0))
         sim.update(1 / 60)
-    zero = ws.warm_start_solve(sim, None, mask, rtol=1e-3, check=50, time_limit_s=60)
-    warm = ws.warm_start_solve(sim, net, mask, rtol=1e-3, check=50, time_limit_s=60)
+    regions = ws.Regions(mask.view(1, size, -1), 1, size, size)
+    ws.project_divergence(sim, regions)
+    b = sim.divergence.double()
+    for k in range(regions.n):
+        sel = regions.labels[0] == k
+        assert abs(float(b[sel].mean())) <= 1e-6 * float(b[sel].abs().max()) + 1e-12
+    floor = ws.fp32_floor(sim, regions)
+    assert floor < 1e-4, floor  # FP32 storage of the exact solution at 128x128
+    zero = ws.warm_start_solve(sim, None, mask, rtol=1e-3, check=50, time_limit_s=60,
+                               regions=regions)
+    warm = ws.warm_start_solve(sim, net, mask, rtol=1e-3, check=50, time_limit_s=60,
+                               regions=regions)
     with capsys.disabled():
         print(f"\nwarm start at {size}x{size}: zero {zero['sweeps']} sweeps, network "
               f"{warm['sweeps']} sweeps (fallback {warm['fallback']}); loss {first:.4g} -> {last:.4g}")
