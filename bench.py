@@ -12,7 +12,7 @@ One JSON line on rank 0.  `value` is timed with CUDA events on the launching
 stream with the fields resident on the device (the per-step forcing records,
 ~1.5 KB, go through the API's pinned staging as they would for any caller).
 `e2e` adds, every step, a device->host read of the density frame into pinned
-host memory through the C ABI and the wait for it.  `roofline` is the Jacobi
+host memory through the C ABI (on a copy stream, overlapping the next step).  `roofline` is the Jacobi
 phase (the dominant kernel), timed live with CUDA events around its launches.
 `cpu_baseline` times the CPU oracle (float32, all host threads) on a bounded
 sample of the same workload.  `--impl reference` times that CPU
@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import argparse
 import csv
+import ctypes
 import json
 import os
 import subprocess
@@ -261,21 +262,31 @@ def run_natrix(args, spec):
     sim.sync()
     launches = int(stats.kernel_launches)
 
-    # e2e: the same frames through the C ABI with a device->host read of
-    # every frame's density into pinned host memory, waited on each step
-    host = torch.empty((H, W), dtype=torch.float32).pin_memory()
-    hp = host.data_ptr()
-    import ctypes
-
-    hptr = ctypes.c_void_p(hp)
-    sptr = ctypes.c_void_p(stream.cuda_stream)
+    # e2e: the same frames through the C ABI, each frame's density read back
+    # into pinned host memory.  The read of frame k runs on a copy stream
+    # while frame k+1 computes (frame k+1 only reads that buffer); frame k+2,
+    # which overwrites it, waits for the copy.  The clock stops after the
+    # last copy has landed.
+    hosts = [torch.empty((H, W), dtype=torch.float32).pin_memory() for _ in range(2)]
+    hptrs = [ctypes.c_void_p(h.data_ptr()) for h in hosts]
+    copy_stream = torch.cuda.Stream()
+    cptr = ctypes.c_void_p(copy_stream.cuda_stream)
+    copied = [None, None]
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
-    for i in range(args.warmup + args.steps, total):
+    for k, i in enumerate(range(args.warmup + args.steps, total)):
+        if copied[k % 2] is not None:
+            stream.wait_event(copied[k % 2])
         frame(i)
-        _lib.check(lib.natrix_density_download(den.handle, hptr, sptr))
-        stream.synchronize()
+        ready = torch.cuda.Event()
+        ready.record(stream)
+        copy_stream.wait_event(ready)
+        _lib.check(lib.natrix_density_download(den.handle, hptrs[k % 2], cptr))
+        copied[k % 2] = torch.cuda.Event()
+        copied[k % 2].record(copy_stream)
+    copy_stream.synchronize()
+    stream.synchronize()
     t_e2e = time.perf_counter() - t0
     barrier()
     sim.sync()
@@ -598,6 +609,85 @@ def run_warmstart(args):
     print(json.dumps(line), flush=True)
 
 
+def run_render(args):
+    """Headless display of a 2048x2048 density frame: texture + plasma colour
+    (12 bytes per pixel: 4 read, 8 written) and a 4096x4096 quiver overlay of
+    the velocity (16-pixel tiles), timed with CUDA events per frame."""
+    import torch
+
+    from natrix_gb300 import FluidSimulator, SmoothParticlesArea, render
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    spec = make_spec("large")
+    W, H = spec.width, spec.height
+    sim = FluidSimulator(W, H)
+    den = SmoothParticlesArea(W, H, sim)
+    sim.iterations, sim.vorticity, sim.viscosity, sim.speed, sim.dissipation = (
+        spec.iterations, spec.vorticity, spec.viscosity, spec.speed, spec.dissipation)
+    den.speed, den.dissipation = spec.speed, spec.dissipation
+    rng = np.random.default_rng(3)
+    for _ in range(5):
+        sim.add_splats(wl.gauss_splats(rng, spec.splats_per_step, W, H, spec.speed), den)
+        sim.update(spec.dt)
+        den.update(spec.dt)
+    rho = den.density
+    vel = sim.get_velocity_buffer()
+    tex = torch.empty(H, W, 4, dtype=torch.uint8, device="cuda")
+    col = torch.empty_like(tex)
+    win = (2 * W, 2 * H)
+    nx, ny = render.quiver_tiles(win, 16.0)
+    arrows = torch.empty(ny, nx, 2, device="cuda")
+    ov = torch.empty(win[1], win[0], 4, dtype=torch.uint8, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    from natrix_gb300._lib import load as natrix_lib
+
+    lib = natrix_lib()
+
+    def density_frame():
+        return lib.natrix_render_density(ctypes.c_void_p(rho.data_ptr()), W, H, rho.stride(0),
+                                  ctypes.c_void_p(tex.data_ptr()), ctypes.c_void_p(col.data_ptr()),
+                                  W, st)
+
+    def quiver_frame():
+        return lib.natrix_quiver(ctypes.c_void_p(vel.data_ptr()), W, H, vel.stride(0) // 2, win[0],
+                          win[1], ctypes.c_float(16.0), ctypes.c_void_p(arrows.data_ptr()),
+                          ctypes.c_void_p(ov.data_ptr()), win[0], st)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            if fn() != 0:
+                raise RuntimeError(lib.natrix_last_error().decode())
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    d_ms, q_ms = timed(density_frame), timed(quiver_frame)
+    hbm, kind = load_peaks()
+    d_bytes = 12.0 * W * H
+    q_bytes = 4.0 * win[0] * win[1]
+    line = {
+        "metric": "density frames/s (2048x2048 texture + colour)", "value": 1e3 / d_ms,
+        "unit": "frames/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": d_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u8 (f32 in)", "data": "synthetic (solver frames)",
+        "config": {"workload": "render-2048x2048+quiver-4096x4096-tile16",
+                   "l2": "density 16.8 MB read, 33.6 MB written per frame (< L2)"},
+        "roofline": {"bound": "hbm", "achieved": d_bytes / d_ms / 1e6, "peak": hbm,
+                     "unit": "GB/s", "frac": d_bytes / d_ms / 1e6 / hbm, "traffic": None,
+                     "peak_kind": kind},
+        "quiver": {"ms": q_ms, "gbs": q_bytes / q_ms / 1e6, "frac": q_bytes / q_ms / 1e6 / hbm,
+                   "window": list(win), "tiles": [nx, ny]},
+    }
+    print(json.dumps(line), flush=True)
+    den.destroy()
+    sim.destroy()
+
+
 def run_unet_forward(args):
     """Warm-start network inference throughput: one forward pass of
     --batch x 512 x 512 (synthetic divergence and obstacle fields) per step,
@@ -653,7 +743,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["natrix", "reference"], default="natrix")
     ap.add_argument("--workload", choices=["large", "small", "particles", "batch", "warmstart",
-                                           "unet-forward"], default="large")
+                                           "unet-forward", "render"], default="large")
     ap.add_argument("--batch", type=int, default=64, help="unet-forward: images per pass")
     ap.add_argument("--pairs", type=int, default=512, help="warmstart: training pairs")
     ap.add_argument("--train-steps", type=int, default=400, help="warmstart: Adam steps")
@@ -671,6 +761,9 @@ def main():
         return
     if args.workload == "unet-forward":
         run_unet_forward(args)
+        return
+    if args.workload == "render":
+        run_render(args)
         return
     spec = make_spec(args.workload)
     if args.impl == "reference":

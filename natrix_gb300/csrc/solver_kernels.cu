@@ -16,7 +16,7 @@ inline dim3 grid_for(const Grid& g) { return dim3((g.W + BX - 1) / BX, (g.H + BY
 // The streaming stencil kernels give each thread CPT cells of one column,
 // BY rows apart, so every thread has CPT independent load chains in flight
 // (one 8-byte load per thread per block leaves HBM under-subscribed).
-constexpr int CPT = 2;
+constexpr int CPT = 4;
 inline dim3 grid_cpt(const Grid& g) {
     return dim3((g.W + BX - 1) / BX, (g.H + BY * CPT - 1) / (BY * CPT));
 }
