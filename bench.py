@@ -688,6 +688,44 @@ def run_render(args):
     sim.destroy()
 
 
+def run_unet_train(args):
+    """Warm-start network training throughput: Adam steps (forward, loss,
+    backward, update) on --batch x 512 x 512 synthetic inputs against a fixed
+    synthetic target, timed with CUDA events; the training images/s the
+    warm-start leg reports, without its data generation."""
+    import torch
+
+    from natrix_gb300.core import warmstart as ws
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    B, H, W = args.batch, 512, 512
+    P = (W + 31) // 32 * 32
+    g = torch.Generator(device="cuda").manual_seed(0)
+    div = torch.randn(B, H, P, device="cuda", generator=g)
+    mask = (torch.rand(B, H, P, device="cuda", generator=g) < 0.05).to(torch.uint8)
+    inv = ws.inv_scale_of(div[:, :, :W], mask[:, :, :W])
+    target = torch.randn(B, H, W, device="cuda", generator=g)
+    net = ws.UNet(seed=0)
+    for _ in range(args.warmup):
+        net.train_step(div, mask, inv, target, H, W, P)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        net.train_step(div, mask, inv, target, H, W, P)
+    e1.record()
+    torch.cuda.synchronize()
+    net.check_status()
+    ms = e0.elapsed_time(e1) / args.steps
+    print(json.dumps({
+        "metric": "U-Net training images/s (512x512)", "value": B / ms * 1e3, "unit": "images/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 (f32 accumulate, f32 master weights)", "data": "synthetic",
+        "config": {"workload": f"unet-train-{B}x512x512", "batch": B, "optimizer": "adam"},
+    }), flush=True)
+
+
 def run_unet_forward(args):
     """Warm-start network inference throughput: one forward pass of
     --batch x 512 x 512 (synthetic divergence and obstacle fields) per step,
@@ -743,7 +781,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["natrix", "reference"], default="natrix")
     ap.add_argument("--workload", choices=["large", "small", "particles", "batch", "warmstart",
-                                           "unet-forward", "render"], default="large")
+                                           "unet-forward", "unet-train", "render"],
+                    default="large")
     ap.add_argument("--batch", type=int, default=64, help="unet-forward: images per pass")
     ap.add_argument("--pairs", type=int, default=512, help="warmstart: training pairs")
     ap.add_argument("--train-steps", type=int, default=400, help="warmstart: Adam steps")
@@ -761,6 +800,9 @@ def main():
         return
     if args.workload == "unet-forward":
         run_unet_forward(args)
+        return
+    if args.workload == "unet-train":
+        run_unet_train(args)
         return
     if args.workload == "render":
         run_render(args)

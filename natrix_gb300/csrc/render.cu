@@ -226,6 +226,75 @@ __global__ void __launch_bounds__(kRenderThreads)
     }
 }
 
+// Integer tile sizes: one block per tile.  The arrow's three segments (shaft
+// and two head strokes) depend only on the tile, so one thread evaluates
+// _line's per-segment terms (centre, direction, half length) once and every
+// pixel does the two dot products; the values are those arrow_dist computes,
+// so the overlay is identical to the per-pixel kernel's.
+struct Seg {
+    float cx, cy, dx, dy, hl;
+};
+
+__device__ Seg make_seg(float ax, float ay, float bx, float by) {
+    Seg s;
+    s.cx = (ax + bx) * 0.5f;
+    s.cy = (ay + by) * 0.5f;
+    const float ex = bx - ax, ey = by - ay;
+    const float len = len2(ex, ey);
+    s.dx = ex / len;
+    s.dy = ey / len;
+    s.hl = 0.5f * len;
+    return s;
+}
+
+__device__ __forceinline__ float seg_dist(const Seg& s, float px, float py) {
+    const float rx = px - s.cx, ry = py - s.cy;
+    const float d1 = fabsf(rx * s.dy + ry * -s.dx);
+    const float d2 = fabsf(rx * s.dx + ry * s.dy) - s.hl;
+    return fmaxf(d1, d2);
+}
+
+__global__ void __launch_bounds__(kRenderThreads)
+    k_quiver_overlay_tiles(const float2* __restrict__ arrows, QuiverGeom g, int W, int H, int T,
+                           uchar4* __restrict__ out, long opitch) {
+    __shared__ Seg segs[3];
+    __shared__ int s_live;
+    for (long tile = blockIdx.x; tile < (long)g.nx * g.ny; tile += gridDim.x) {
+        const int ti = (int)(tile % g.nx), tj = (int)(tile / g.nx);
+        if (threadIdx.x == 0) {
+            float vx = arrows[tile].x, vy = arrows[tile].y;
+            float mag = len2(vx, vy);
+            s_live = mag > 0.001f;
+            if (s_live) {
+                const float ux = vx / mag, uy = vy / mag;
+                mag = fminf(fmaxf(mag, 0.0f), g.T * 0.5f);
+                vx = ux * mag;
+                vy = uy * mag;
+                segs[0] = make_seg(vx, vy, -vx, -vy);
+                segs[1] = make_seg(vx, vy, 0.4f * vx + 0.2f * -vy, 0.4f * vy + 0.2f * vx);
+                segs[2] = make_seg(vx, vy, 0.4f * vx + 0.2f * vy, 0.4f * vy + 0.2f * -vx);
+            }
+        }
+        __syncthreads();
+        const float cx = ((float)ti + 0.5f) * g.T, cy = ((float)tj + 0.5f) * g.T;
+        const int x0 = ti * T, y0 = tj * T;
+        const bool live = s_live != 0;
+        for (int k = threadIdx.x; k < T * T; k += kRenderThreads) {
+            const int x = x0 + k % T, y = y0 + k / T;
+            if (x >= W || y >= H) continue;
+            float d = 1.0f;
+            if (live) {
+                const float px = ((float)x + 0.5f) - cx, py = ((float)y + 0.5f) - cy;
+                d = fminf(seg_dist(segs[0], px, py),
+                          fminf(seg_dist(segs[1], px, py), seg_dist(segs[2], px, py)));
+            }
+            const float alpha = 1.0f - fminf(fmaxf(d, 0.0f), 1.0f);
+            out[(long)y * opitch + x] = make_uchar4(255, 255, 255, unorm8(alpha));
+        }
+        __syncthreads();
+    }
+}
+
 int fail(int code, const char* msg) { return set_last_error(code, msg); }
 
 int cuda_fail(cudaError_t e) { return set_last_error(NATRIX_ECUDA, cudaGetErrorString(e)); }
@@ -304,10 +373,18 @@ int natrix_quiver(const float* velocity, int32_t W, int32_t H, int64_t pitch, in
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e);
     if (overlay) {
-        const long px = (long)win_w * win_h;
-        k_quiver_overlay<<<grid_blocks(px), kRenderThreads, 0, st>>>(
-            reinterpret_cast<const float2*>(arrows), g, win_w, win_h,
-            reinterpret_cast<uchar4*>(overlay), overlay_pitch);
+        const int ti = (int)tile;
+        if ((float)ti == tile && ti <= 256) {
+            const long nt = tiles < 65535L * 8 ? tiles : 65535L * 8;
+            k_quiver_overlay_tiles<<<(unsigned)nt, kRenderThreads, 0, st>>>(
+                reinterpret_cast<const float2*>(arrows), g, win_w, win_h, ti,
+                reinterpret_cast<uchar4*>(overlay), overlay_pitch);
+        } else {
+            const long px = (long)win_w * win_h;
+            k_quiver_overlay<<<grid_blocks(px), kRenderThreads, 0, st>>>(
+                reinterpret_cast<const float2*>(arrows), g, win_w, win_h,
+                reinterpret_cast<uchar4*>(overlay), overlay_pitch);
+        }
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e);
     }
     return NATRIX_OK;

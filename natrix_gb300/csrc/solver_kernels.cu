@@ -142,6 +142,152 @@ __global__ void __launch_bounds__(BX* BY)
     }
 }
 
+// Row-streaming 5-point stencils (divergence, gradient subtraction).  A warp
+// owns 64 consecutive columns (two per lane, so every row is one 16-byte
+// velocity load, one 8-byte scalar load and one 2-byte mask load per lane)
+// and walks ST_ROWS rows down, keeping the rows above and below in
+// registers; the left / right neighbours come from the adjacent lanes by
+// shuffle, and the warp's two edge lanes load the one column beyond.  Each
+// cell's arithmetic is cell_divergence / cell_subtract_gradient's, so the
+// results are identical; these kernels need an even width (the host falls
+// back to the per-cell kernels otherwise).
+constexpr int ST_WARPS = 4, ST_COLS = 64 * ST_WARPS, ST_ROWS = 16;
+
+struct VRow {  // velocity and obstacle flag of a lane's two cells
+    float2 a, b;
+    uint8_t ma, mb;
+};
+
+__device__ __forceinline__ VRow load_vrow(const float2* __restrict__ v,
+                                          const uint8_t* __restrict__ mask, const Grid& g, int y,
+                                          int c, bool mz) {
+    y = min(max(y, 0), g.H - 1);
+    VRow r;
+    const float4 q = __ldg(reinterpret_cast<const float4*>(v + (size_t)y * g.P + c));
+    r.a = make_float2(q.x, q.y);
+    r.b = make_float2(q.z, q.w);
+    if (mz) {
+        r.ma = r.mb = 0;
+    } else {
+        const uint16_t m = __ldg(reinterpret_cast<const uint16_t*>(mask + (size_t)y * g.P + c));
+        r.ma = (uint8_t)(m & 0xff);
+        r.mb = (uint8_t)(m >> 8);
+    }
+    return r;
+}
+
+__global__ void __launch_bounds__(32 * ST_WARPS)
+    k_divergence_st(const float2* __restrict__ v, const uint8_t* __restrict__ mask,
+                    float* __restrict__ div, uint8_t* __restrict__ flags, float* __restrict__ p1,
+                    Grid g, const StepParams* __restrict__ sp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = blockIdx.x * ST_COLS + warp * 64 + 2 * lane;  // this lane's first column
+    const int y0 = blockIdx.y * ST_ROWS;
+    const bool live = c < g.W;  // W even: c + 1 < W too
+    const int cc = live ? c : g.W - 2;  // dead lanes load a valid pair
+    const bool mz = sp->mask_zero != 0;
+    const unsigned FULL = 0xffffffffu;
+    VRow up = load_vrow(v, mask, g, y0 - 1, cc, mz);
+    VRow mid = load_vrow(v, mask, g, y0, cc, mz);
+    const int y1 = min(y0 + ST_ROWS, g.H);
+    for (int y = y0; y < y1; ++y) {
+        const VRow dn = load_vrow(v, mask, g, y + 1, cc, mz);
+        // left neighbour of column c (clamped), right neighbour of c + 1
+        float lx = __shfl_up_sync(FULL, mid.b.x, 1);
+        uint8_t lm = (uint8_t)__shfl_up_sync(FULL, (int)mid.mb, 1);
+        float rx = __shfl_down_sync(FULL, mid.a.x, 1);
+        uint8_t rm = (uint8_t)__shfl_down_sync(FULL, (int)mid.ma, 1);
+        const size_t row = (size_t)y * g.P;
+        if (lane == 0) {
+            const int xl = max(cc - 1, 0);
+            lx = __ldg(v + row + xl).x;
+            lm = mz ? 0 : __ldg(mask + row + xl);
+        }
+        if (lane == 31 || cc + 2 >= g.W) {
+            const int xr = min(cc + 2, g.W - 1);
+            rx = __ldg(v + row + xr).x;
+            rm = mz ? 0 : __ldg(mask + row + xr);
+        }
+        if (live) {
+            // cell c: left = lx/lm, right = c+1; cell c+1: left = c, right = rx/rm
+            const bool ol0 = lm != 0, or0 = mid.mb != 0, ob0 = up.ma != 0, ot0 = dn.ma != 0;
+            const bool ol1 = mid.ma != 0, or1 = rm != 0, ob1 = up.mb != 0, ot1 = dn.mb != 0;
+            const float b0 = 0.5f * (((or0 ? 0.0f : mid.b.x) - (ol0 ? 0.0f : lx)) +
+                                     ((ot0 ? 0.0f : dn.a.y) - (ob0 ? 0.0f : up.a.y)));
+            const float b1 = 0.5f * (((or1 ? 0.0f : rx) - (ol1 ? 0.0f : mid.a.x)) +
+                                     ((ot1 ? 0.0f : dn.b.y) - (ob1 ? 0.0f : up.b.y)));
+            *reinterpret_cast<float2*>(div + row + c) = make_float2(b0, b1);
+            uint8_t f0 = 0, f1 = 0;
+            if (c == 0 || ol0) f0 |= NB_L;
+            if (or0) f0 |= NB_R;
+            if (y == 0 || ob0) f0 |= NB_B;
+            if (y == g.H - 1 || ot0) f0 |= NB_T;
+            if (ol1) f1 |= NB_L;
+            if (c + 1 == g.W - 1 || or1) f1 |= NB_R;
+            if (y == 0 || ob1) f1 |= NB_B;
+            if (y == g.H - 1 || ot1) f1 |= NB_T;
+            *reinterpret_cast<uint16_t*>(flags + row + c) = (uint16_t)(f0 | (f1 << 8));
+            if (p1)
+                *reinterpret_cast<float2*>(p1 + row + c) =
+                    make_float2((0.0f - b0) * 0.25f, (0.0f - b1) * 0.25f);
+        }
+        up = mid;
+        mid = dn;
+    }
+}
+
+__global__ void __launch_bounds__(32 * ST_WARPS)
+    k_subtract_gradient_st(const float2* __restrict__ vin, float2* __restrict__ vout,
+                           const float* __restrict__ p, const uint8_t* __restrict__ flags, Grid g) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = blockIdx.x * ST_COLS + warp * 64 + 2 * lane;
+    const int y0 = blockIdx.y * ST_ROWS;
+    const bool live = c < g.W;
+    const int cc = live ? c : g.W - 2;
+    const unsigned FULL = 0xffffffffu;
+    auto prow = [&](int y) {
+        y = min(max(y, 0), g.H - 1);
+        return __ldg(reinterpret_cast<const float2*>(p + (size_t)y * g.P + cc));
+    };
+    float2 up = prow(y0 - 1), mid = prow(y0);
+    const int y1 = min(y0 + ST_ROWS, g.H);
+    for (int y = y0; y < y1; ++y) {
+        const float2 dn = prow(y + 1);
+        const size_t row = (size_t)y * g.P;
+        float lp = __shfl_up_sync(FULL, mid.y, 1);
+        float rp = __shfl_down_sync(FULL, mid.x, 1);
+        if (lane == 0) lp = __ldg(p + row + max(cc - 1, 0));
+        if (lane == 31 || cc + 2 >= g.W) rp = __ldg(p + row + min(cc + 2, g.W - 1));
+        if (live) {
+            const uint16_t fw = *reinterpret_cast<const uint16_t*>(flags + row + c);
+            const uint8_t f0 = (uint8_t)(fw & 0xff), f1 = (uint8_t)(fw >> 8);
+            const float4 q = *reinterpret_cast<const float4*>(vin + row + c);
+            float2 v0 = make_float2(q.x, q.y), v1 = make_float2(q.z, q.w);
+            {
+                const float pc = mid.x;
+                const float x1 = (f0 & NB_L) ? pc : lp;
+                const float x2 = (f0 & NB_R) ? pc : mid.y;
+                const float yb = (f0 & NB_B) ? pc : up.x;
+                const float yt = (f0 & NB_T) ? pc : dn.x;
+                v0.x -= 0.5f * (x2 - x1);
+                v0.y -= 0.5f * (yt - yb);
+            }
+            {
+                const float pc = mid.y;
+                const float x1 = (f1 & NB_L) ? pc : mid.x;
+                const float x2 = (f1 & NB_R) ? pc : rp;
+                const float yb = (f1 & NB_B) ? pc : up.y;
+                const float yt = (f1 & NB_T) ? pc : dn.y;
+                v1.x -= 0.5f * (x2 - x1);
+                v1.y -= 0.5f * (yt - yb);
+            }
+            *reinterpret_cast<float4*>(vout + row + c) = make_float4(v0.x, v0.y, v1.x, v1.y);
+        }
+        up = mid;
+        mid = dn;
+    }
+}
+
 // ----------------------------------------------------------------- residual
 // r = b - (sum of substituted neighbours - 4 p) over fluid cells, in double;
 // warp-shuffle then shared-memory reduction per block, block partials summed
@@ -322,13 +468,21 @@ cudaError_t launch_viscosity(const float2* vin, float2* vout, Grid g, const Step
 cudaError_t launch_divergence(const float2* v, const uint8_t* mask, float* div,
                               uint8_t* flags, float* p1, Grid g, const StepParams* sp,
                               cudaStream_t st) {
-    k_divergence<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(v, mask, div, flags, p1, g, sp);
+    if (g.W % 2 == 0 && g.W >= 2)
+        k_divergence_st<<<dim3((g.W + ST_COLS - 1) / ST_COLS, (g.H + ST_ROWS - 1) / ST_ROWS),
+                          32 * ST_WARPS, 0, st>>>(v, mask, div, flags, p1, g, sp);
+    else
+        k_divergence<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(v, mask, div, flags, p1, g, sp);
     return cudaGetLastError();
 }
 
 cudaError_t launch_subtract_gradient(const float2* vin, float2* vout, const float* p,
                                      const uint8_t* flags, Grid g, cudaStream_t st) {
-    k_subtract_gradient<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(vin, vout, p, flags, g);
+    if (g.W % 2 == 0 && g.W >= 2)
+        k_subtract_gradient_st<<<dim3((g.W + ST_COLS - 1) / ST_COLS, (g.H + ST_ROWS - 1) / ST_ROWS),
+                                 32 * ST_WARPS, 0, st>>>(vin, vout, p, flags, g);
+    else
+        k_subtract_gradient<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(vin, vout, p, flags, g);
     return cudaGetLastError();
 }
 

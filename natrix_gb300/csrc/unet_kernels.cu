@@ -108,24 +108,47 @@ __global__ void __launch_bounds__(256)
         }
         for (long base = p0; base < p1; base += WG_PIX) {
             __syncthreads();
-            for (int i = threadIdx.x; i < WG_PIX * cout; i += 256) {
-                const long p = base + i / cout;
-                sdz[i] = p < p1 ? bf(dz[p * cout + i % cout]) : 0.0f;
+            // stage WG_PIX pixels: 8 channels (16 bytes) per load, 32-bit indices
+            const int cz8 = cout / 8, ci8 = cin / 8, c08 = c0 / 8;
+            for (int i = threadIdx.x; i < WG_PIX * cz8; i += 256) {
+                const int k = i / cz8, q = i % cz8;
+                const int p = (int)base + k;
+                float* d = sdz + k * cout + 8 * q;
+                if (p < (int)p1) {
+                    const uint4 u = *reinterpret_cast<const uint4*>(dz + (size_t)p * cout + 8 * q);
+                    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        d[2 * j] = bf((uint16_t)(w[j] & 0xffffu));
+                        d[2 * j + 1] = bf((uint16_t)(w[j] >> 16));
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) d[j] = 0.0f;
+                }
             }
-            for (int i = threadIdx.x; i < WG_PIX * cin; i += 256) {
-                const long p = base + i / cin;
-                const int c = i % cin;
-                float v = 0.0f;
-                if (p < p1) {
-                    const int xx = (int)(p % W), yy = (int)((p / W) % H);
-                    const long bb = p / ((long)W * H);
+            for (int i = threadIdx.x; i < WG_PIX * ci8; i += 256) {
+                const int k = i / ci8, q = i % ci8;
+                const int p = (int)base + k;
+                float* d = sx + k * cin + 8 * q;
+                uint4 u = make_uint4(0, 0, 0, 0);
+                if (p < (int)p1) {
+                    const int xx = p % W, yb = p / W;
+                    const int yy = yb % H, bb = yb / H;
                     const int sx_ = xx + dx, sy_ = yy + dy;
                     if (sx_ >= 0 && sx_ < W && sy_ >= 0 && sy_ < H) {
-                        const long q = (bb * H + sy_) * W + sx_;
-                        v = c < c0 ? bf(x0[q * c0 + c]) : bf(x1[q * c1 + (c - c0)]);
+                        const int src = (bb * H + sy_) * W + sx_;
+                        u = q < c08 ? *reinterpret_cast<const uint4*>(x0 + (size_t)src * c0 + 8 * q)
+                                    : *reinterpret_cast<const uint4*>(x1 + (size_t)src * c1 +
+                                                                       8 * (q - c08));
                     }
                 }
-                sx[i] = v;
+                const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    d[2 * j] = bf((uint16_t)(w[j] & 0xffffu));
+                    d[2 * j + 1] = bf((uint16_t)(w[j] >> 16));
+                }
             }
             __syncthreads();
             if (mine) {
@@ -185,70 +208,117 @@ __global__ void k_prep(const float* __restrict__ div, const uint8_t* __restrict_
     }
 }
 
-// 2x2 average pooling, stride 2 (H, W even)
+// Pooling / upsampling and their gradients on NHWC bf16 tensors, eight
+// channels (16 bytes) per thread, 32-bit pixel indices (C is a multiple of 8).
+struct Bf8 {
+    float v[8];
+};
+
+__device__ __forceinline__ Bf8 ld8(const uint16_t* p) {
+    const uint4 q = *reinterpret_cast<const uint4*>(p);
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+    Bf8 r;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        r.v[2 * j] = bf((uint16_t)(w[j] & 0xffffu));
+        r.v[2 * j + 1] = bf((uint16_t)(w[j] >> 16));
+    }
+    return r;
+}
+
+__device__ __forceinline__ void st8(uint16_t* p, const Bf8& r) {
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        w[j] = (uint32_t)tobf(r.v[2 * j]) | ((uint32_t)tobf(r.v[2 * j + 1]) << 16);
+    *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// 2x2 average pooling: one thread per output pixel and 8-channel chunk
 __global__ void k_pool(const uint16_t* __restrict__ in, int B, int H, int W, int C,
                        uint16_t* __restrict__ out) {
-    const int Ho = H / 2, Wo = W / 2;
-    const long n = (long)B * Ho * Wo * C;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-         i += (long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long p = i / C;
-        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
-        const long b = p / ((long)Wo * Ho);
-        const long q = (b * H + 2 * y) * W + 2 * x;
-        const float s = bf(in[q * C + c]) + bf(in[(q + 1) * C + c]) + bf(in[(q + W) * C + c]) +
-                        bf(in[(q + W + 1) * C + c]);
-        out[i] = tobf(0.25f * s);
+    const int Ho = H / 2, Wo = W / 2, CC = C / 8;
+    const int n = B * Ho * Wo * CC;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int q = i % CC, p = i / CC;
+        const int x = p % Wo, yb = p / Wo;  // yb = b * Ho + y
+        const int y = yb % Ho, b = yb / Ho;
+        const int src = (b * H + 2 * y) * W + 2 * x;
+        const Bf8 a = ld8(in + (size_t)src * C + 8 * q), c = ld8(in + (size_t)(src + 1) * C + 8 * q),
+                  d = ld8(in + (size_t)(src + W) * C + 8 * q),
+                  e = ld8(in + (size_t)(src + W + 1) * C + 8 * q);
+        Bf8 r;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) r.v[j] = 0.25f * (((a.v[j] + c.v[j]) + d.v[j]) + e.v[j]);
+        st8(out + (size_t)i * 8, r);
     }
 }
 
-// nearest upsampling x2
+// nearest upsampling x2: one thread per input pixel and chunk, four stores
 __global__ void k_up(const uint16_t* __restrict__ in, int B, int H, int W, int C,
                      uint16_t* __restrict__ out) {
-    const int Ho = 2 * H, Wo = 2 * W;
-    const long n = (long)B * Ho * Wo * C;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-         i += (long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long p = i / C;
-        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
-        const long b = p / ((long)Wo * Ho);
-        out[i] = in[(((b * H + y / 2) * W) + x / 2) * C + c];
+    const int CC = C / 8, Wo = 2 * W;
+    const int n = B * H * W * CC;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int q = i % CC, p = i / CC;
+        const int x = p % W, yb = p / W;  // yb = b * H + y
+        const uint4 v = *reinterpret_cast<const uint4*>(in + (size_t)i * 8);
+        const int dst = (2 * yb) * Wo + 2 * x;  // (b * 2H + 2y) * 2W + 2x
+        *reinterpret_cast<uint4*>(out + (size_t)dst * C + 8 * q) = v;
+        *reinterpret_cast<uint4*>(out + (size_t)(dst + 1) * C + 8 * q) = v;
+        *reinterpret_cast<uint4*>(out + (size_t)(dst + Wo) * C + 8 * q) = v;
+        *reinterpret_cast<uint4*>(out + (size_t)(dst + Wo + 1) * C + 8 * q) = v;
     }
 }
 
 // gradient of nearest upsampling (sum of the 4 children), times (gate > 0)
 __global__ void k_up_back(const uint16_t* __restrict__ dup, int B, int H, int W, int C,
                           const uint16_t* __restrict__ gate, uint16_t* __restrict__ out) {
-    const long n = (long)B * H * W * C;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-         i += (long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long p = i / C;
-        const int x = (int)(p % W), y = (int)((p / W) % H);
-        const long b = p / ((long)W * H);
-        const long q = (b * 2 * H + 2 * y) * (2 * W) + 2 * x;
-        const float s = bf(dup[q * C + c]) + bf(dup[(q + 1) * C + c]) +
-                        bf(dup[(q + 2 * W) * C + c]) + bf(dup[(q + 2 * W + 1) * C + c]);
-        out[i] = bf(gate[i]) > 0.0f ? tobf(s) : (uint16_t)0;
+    const int CC = C / 8, Wf = 2 * W;
+    const int n = B * H * W * CC;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int q = i % CC, p = i / CC;
+        const int x = p % W, yb = p / W;
+        const int src = (2 * yb) * Wf + 2 * x;
+        const Bf8 a = ld8(dup + (size_t)src * C + 8 * q), c = ld8(dup + (size_t)(src + 1) * C + 8 * q),
+                  d = ld8(dup + (size_t)(src + Wf) * C + 8 * q),
+                  e = ld8(dup + (size_t)(src + Wf + 1) * C + 8 * q);
+        const Bf8 g = ld8(gate + (size_t)i * 8);
+        Bf8 r;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float s = ((a.v[j] + c.v[j]) + d.v[j]) + e.v[j];
+            r.v[j] = g.v[j] > 0.0f ? s : 0.0f;
+        }
+        st8(out + (size_t)i * 8, r);
     }
 }
 
-// (skip + gradient of 2x2 average pooling) times (gate > 0)
+// (skip + gradient of 2x2 average pooling) times (gate > 0): one thread per
+// coarse pixel and chunk, writing its four fine pixels
 __global__ void k_pool_back(const uint16_t* __restrict__ skip, const uint16_t* __restrict__ dq,
                             int B, int H, int W, int C, const uint16_t* __restrict__ gate,
                             uint16_t* __restrict__ out) {
-    const long n = (long)B * H * W * C;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-         i += (long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long p = i / C;
-        const int x = (int)(p % W), y = (int)((p / W) % H);
-        const long b = p / ((long)W * H);
-        const long q = (b * (H / 2) + y / 2) * (W / 2) + x / 2;
-        const float s = bf(skip[i]) + 0.25f * bf(dq[q * C + c]);
-        out[i] = bf(gate[i]) > 0.0f ? tobf(s) : (uint16_t)0;
+    const int Hc = H / 2, Wc = W / 2, CC = C / 8;
+    const int n = B * Hc * Wc * CC;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int q = i % CC, p = i / CC;
+        const int x = p % Wc, yb = p / Wc;  // yb = b * Hc + y
+        const Bf8 d = ld8(dq + (size_t)i * 8);
+        const int base = (2 * yb) * W + 2 * x;  // (b * H + 2y) * W + 2x
+        const int fine[4] = {base, base + 1, base + W, base + W + 1};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const size_t o = (size_t)fine[k] * C + 8 * q;
+            const Bf8 sk = ld8(skip + o), g = ld8(gate + o);
+            Bf8 r;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float s = sk.v[j] + 0.25f * d.v[j];
+                r.v[j] = g.v[j] > 0.0f ? s : 0.0f;
+            }
+            st8(out + o, r);
+        }
     }
 }
 
@@ -507,6 +577,9 @@ int natrix_nn_wgrad(const uint16_t* dz, int32_t cout, const uint16_t* x0, int32_
                     float* db, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const long npix = (long)B * H * W;
+    if (cout % 8 || c0 % 8 || c1 % 8 || (c1 && !x1) || npix >= (1L << 31))
+        return set_last_error(NATRIX_EINVAL, "wgrad: channels must be multiples of 8, "
+                                             "fewer than 2^31 pixels");
     int slices = (int)((npix + 4095) / 4096);
     slices = slices < 1 ? 1 : (slices > 256 ? 256 : slices);
     const size_t smem = (size_t)WG_PIX * (cout + c0 + c1) * sizeof(float);
@@ -526,7 +599,8 @@ int natrix_nn_prep(const float* div, const uint8_t* mask, const float* inv_scale
 int natrix_nn_pool(const uint16_t* in, int32_t B, int32_t H, int32_t W, int32_t C, uint16_t* out,
                    void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const long n = (long)B * (H / 2) * (W / 2) * C;
+    if (C % 8 || H % 2 || W % 2) return set_last_error(NATRIX_EINVAL, "pool: C % 8, H, W even");
+    const long n = (long)B * (H / 2) * (W / 2) * (C / 8);
     k_pool<<<blocks(n, 256) < 8192 ? blocks(n, 256) : 8192, 256, 0, st>>>(in, B, H, W, C, out);
     return launch_status();
 }
@@ -534,7 +608,8 @@ int natrix_nn_pool(const uint16_t* in, int32_t B, int32_t H, int32_t W, int32_t 
 int natrix_nn_up(const uint16_t* in, int32_t B, int32_t H, int32_t W, int32_t C, uint16_t* out,
                  void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const long n = (long)B * 4 * H * W * C;
+    if (C % 8) return set_last_error(NATRIX_EINVAL, "up: C must be a multiple of 8");
+    const long n = (long)B * H * W * (C / 8);
     k_up<<<blocks(n, 256) < 8192 ? blocks(n, 256) : 8192, 256, 0, st>>>(in, B, H, W, C, out);
     return launch_status();
 }
@@ -542,7 +617,8 @@ int natrix_nn_up(const uint16_t* in, int32_t B, int32_t H, int32_t W, int32_t C,
 int natrix_nn_up_back(const uint16_t* dup, int32_t B, int32_t H, int32_t W, int32_t C,
                       const uint16_t* gate, uint16_t* out, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const long n = (long)B * H * W * C;
+    if (C % 8) return set_last_error(NATRIX_EINVAL, "up_back: C must be a multiple of 8");
+    const long n = (long)B * H * W * (C / 8);
     k_up_back<<<blocks(n, 256) < 8192 ? blocks(n, 256) : 8192, 256, 0, st>>>(dup, B, H, W, C,
                                                                             gate, out);
     return launch_status();
@@ -551,7 +627,8 @@ int natrix_nn_up_back(const uint16_t* dup, int32_t B, int32_t H, int32_t W, int3
 int natrix_nn_pool_back(const uint16_t* skip, const uint16_t* dq, int32_t B, int32_t H, int32_t W,
                         int32_t C, const uint16_t* gate, uint16_t* out, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const long n = (long)B * H * W * C;
+    if (C % 8 || H % 2 || W % 2) return set_last_error(NATRIX_EINVAL, "pool_back: C % 8, H, W even");
+    const long n = (long)B * (H / 2) * (W / 2) * (C / 8);
     k_pool_back<<<blocks(n, 256) < 8192 ? blocks(n, 256) : 8192, 256, 0, st>>>(skip, dq, B, H, W,
                                                                               C, gate, out);
     return launch_status();

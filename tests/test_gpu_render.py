@@ -63,8 +63,9 @@ def test_render_live_density_and_quiver(cuda, oracle):
     np.testing.assert_array_equal(col.cpu().numpy(), wc)
     v = sim.get_velocity_buffer().cpu().numpy()
     assert np.abs(v).max() > 0.01
+    # integer tiles take the tile-per-block kernel, 12.5 the per-pixel one
     for window, tile in (((2 * W, 2 * H), 16.0), ((333, 217), 8.0), ((W, H), 64.0),
-                         ((1000, 700), 32.0)):
+                         ((1000, 700), 32.0), ((301, 203), 12.5)):
         arrows, ov = render.quiver(sim, window, tile)
         torch.cuda.synchronize()
         wa, wo = oracle.quiver(v, window[0], window[1], tile)
