@@ -58,10 +58,17 @@ int natrix_nn_pack(const float* w, int32_t cout, int32_t cin, int32_t rows, int3
 
 /* Weight and bias gradients of a 3x3 convolution, accumulated (+=) into
  * dw[cout][cin][3][3] and db[cout] (db may be NULL):
- * dw[co][ci][t] += sum_p dz[p][co] * x[p + offset(t)][ci], x = [x0, x1]. */
+ * dw[co][ci][t] += sum_p dz[p][co] * x[p + offset(t)][ci], x = [x0, x1].
+ * Channel counts are multiples of 8; with cin <= 128 and cout a multiple of
+ * 16 up to 128 the sums run on the tensor cores (one FP32 partial per block,
+ * added atomically), otherwise on the CUDA cores. */
 int natrix_nn_wgrad(const uint16_t* dz, int32_t cout, const uint16_t* x0, int32_t c0,
                     const uint16_t* x1, int32_t c1, int32_t B, int32_t H, int32_t W, float* dw,
                     float* db, void* stream);
+
+/* Status word of the weight-gradient kernels (bit 2 set if a bounded wait
+ * ran out); read and cleared.  Synchronous. */
+int natrix_nn_wgrad_status(int32_t* out);
 
 /* Network input: x[p] = {div[p] * inv_scale[b], obstacle[p], 0 x 6} as
  * 8-channel NHWC bf16 from B pitched float / uint8 fields (mask may be NULL). */

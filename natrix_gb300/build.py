@@ -33,6 +33,7 @@ UNITS = {
     "render.cu": ["-fmad=false"],
     "unet_conv.cu": [],
     "unet_kernels.cu": [],
+    "unet_wgrad.cu": [],
 }
 
 

@@ -52,6 +52,7 @@ _SIGS = {
     "natrix_nn_conv3x3": [ctypes.POINTER(NnConv), _P],
     "natrix_nn_pack": [_P, _I, _I, _I, _I, _I, _P, _P],
     "natrix_nn_wgrad": [_P, _I, _P, _I, _P, _I, _I, _I, _I, _P, _P, _P],
+    "natrix_nn_wgrad_status": [ctypes.POINTER(ctypes.c_int32)],
     "natrix_nn_prep": [_P, _P, _P, _I, _I, _I, _I, _P, _P],
     "natrix_nn_pool": [_P, _I, _I, _I, _I, _P, _P],
     "natrix_nn_up": [_P, _I, _I, _I, _I, _P, _P],
@@ -348,7 +349,9 @@ class UNet:
         c11.gw += self._gw11[:, :c11.cin]
 
     def check_status(self):
-        if int(self.status.item()) != 0:
+        wg = ctypes.c_int32(0)
+        _call("natrix_nn_wgrad_status", ctypes.byref(wg))
+        if int(self.status.item()) != 0 or wg.value != 0:
             self.status.zero_()
             raise _lib.NatrixError(_lib.NATRIX_EDEVICE, "a tensor-core wait ran out")
 

@@ -119,6 +119,11 @@ cudaError_t launch_residual_labels(const float* p, const float* div, const uint8
                                    const int* labels, int n_labels, Grid g, double* sums,
                                    cudaStream_t st);
 
+// ---- U-Net weight gradient on the tensor cores (unet_wgrad.cu) ----
+// cin = c0 + c1 <= 128, cout a multiple of 16 up to 128, channels multiples of 8.
+int wgrad_tc(const uint16_t* dz, int cout, const uint16_t* x0, int c0, const uint16_t* x1, int c1,
+             int B, int H, int W, float* dw, float* db, cudaStream_t st);
+
 // ---- Jacobi (jacobi_tma.cu) ------------------------------------------------
 // Jacobi tile kernels: shared-memory sweeps on 64x32 tiles, or register tiled
 // with 112x112 / 112x128 output tiles.

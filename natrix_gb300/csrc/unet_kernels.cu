@@ -15,6 +15,8 @@
 //    independent system per image, for the training targets.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include "../../include/natrix.h"
 #include "../../include/natrix_nn.h"
 #include "kernels.cuh"
@@ -580,6 +582,8 @@ int natrix_nn_wgrad(const uint16_t* dz, int32_t cout, const uint16_t* x0, int32_
     if (cout % 8 || c0 % 8 || c1 % 8 || (c1 && !x1) || npix >= (1L << 31))
         return set_last_error(NATRIX_EINVAL, "wgrad: channels must be multiples of 8, "
                                              "fewer than 2^31 pixels");
+    if (c0 + c1 <= 128 && cout % 16 == 0 && cout <= 128 && getenv("NATRIX_WGRAD_CUDA_CORES") == nullptr)
+        return wgrad_tc(dz, cout, x0, c0, x1, c1, B, H, W, dw, db, st);
     int slices = (int)((npix + 4095) / 4096);
     slices = slices < 1 ? 1 : (slices > 256 ? 256 : slices);
     const size_t smem = (size_t)WG_PIX * (cout + c0 + c1) * sizeof(float);

@@ -5,6 +5,8 @@ Adam against its formula, the FP64 CG targets against the oracle's residual,
 training progress, and what the trained warm start gains over zero start."""
 from __future__ import annotations
 
+import ctypes
+
 import math
 
 import numpy as np
@@ -114,10 +116,16 @@ def ctypes_byref(c):
     return ctypes.byref(c)
 
 
+@pytest.mark.parametrize("cuda_cores", [False, True])
 @pytest.mark.parametrize("B,H,W,c0,c1,cout", [(2, 8, 40, 16, 0, 32), (1, 12, 24, 64, 32, 32),
-                                              (2, 6, 16, 8, 0, 16)])
-def test_weight_gradient(cuda, B, H, W, c0, c1, cout):
+                                              (2, 6, 16, 8, 0, 16), (3, 20, 70, 32, 16, 64)])
+def test_weight_gradient(cuda, monkeypatch, cuda_cores, B, H, W, c0, c1, cout):
+    """Tensor-core path (default) and CUDA-core path against torch's FP64
+    conv2d_weight; the last shape has 4200 pixels (66 chunks, a partial one)."""
     import torch
+
+    if cuda_cores:
+        monkeypatch.setenv("NATRIX_WGRAD_CUDA_CORES", "1")
 
     from natrix_gb300.core import warmstart as ws
 
@@ -138,6 +146,9 @@ def test_weight_gradient(cuda, B, H, W, c0, c1, cout):
                                        padding=1)
     close(dw, want, rtol=1e-4, what="weight gradient")
     close(db, dz.double().sum((0, 1, 2)), rtol=1e-4, what="bias gradient")
+    st = ctypes.c_int32(0)
+    ws._call("natrix_nn_wgrad_status", ctypes.byref(st))
+    assert st.value == 0
 
 
 def _small_problem(seed=0, B=2, H=32, W=48):
