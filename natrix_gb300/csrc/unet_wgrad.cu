@@ -3,11 +3,12 @@
 // For tap t = (dy, dx):  dW_t[ci][co] = sum over pixels p of
 //     X[p + (dy, dx)][ci] * dZ[p][co]
 // is a GEMM with M = input channels (padded to 128 rows), N = output channels
-// and K = pixels.  Both operands arrive pixel-major (NHWC), so the block
-// transposes chunks of 64 pixels of one image row into the K-major
-// SWIZZLE_NONE operand layout
-// the forward convolution uses (core matrices of 8 rows x 8 pixels, 16-byte
-// rows; SBO = 128 between row groups, LBO between 8-pixel groups): A_dx for
+// and K = pixels.  Both operands arrive pixel-major (NHWC): a producer warp
+// fetches each chunk (64 pixels of one image row, plus one pixel either side
+// of the input rows) with TMA, and eight warps transpose it, 8 x 8 blocks in
+// registers, into the K-major SWIZZLE_NONE operand layout the forward
+// convolution uses (core matrices of 8 rows x 8 pixels, 16-byte rows; SBO =
+// 128 between row groups, LBO between 8-pixel groups): A_dx for
 // the three horizontal taps of one kernel row and B = dZ^T.  One thread issues
 // the 3 x 4 tcgen05.mma (M = 128, N = cout, K = 16) of a chunk into three
 // TMEM accumulators of cout columns; staging and MMAs alternate between two
@@ -16,9 +17,11 @@
 // reads its accumulators with tcgen05.ld and adds them into dW with FP32
 // atomics (one partial sum per block and weight).
 //
-// Pixels outside the image stage as zeros (the convolution's padding).  All
+// Pixels outside the image arrive as zeros from TMA (the convolution's
+// padding).  All
 // waits are bounded; a wait that runs out sets status bit 4 and the block
 // skips the rest of its work after freeing TMEM.
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include "../../include/natrix.h"
@@ -35,7 +38,6 @@ constexpr int kChunkPix = 64;                     // pixels (K) per chunk
 constexpr int kRowsA = 128;                       // M: input channels, padded
 constexpr int kALbo = (kRowsA / 8) * 128;         // 2048 B between 8-pixel groups
 constexpr int kABytes = kRowsA * kChunkPix * 2;   // 16 KB per tap
-constexpr int kBMaxBytes = 128 * kChunkPix * 2;   // cout <= 128
 
 __device__ __forceinline__ float bfw(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
 
@@ -88,35 +90,50 @@ struct WgParams {
     int* status;
     uint32_t tmem_cols;
     uint32_t buf_bytes;  // 3 A tiles + B tile
+    uint32_t raw_bytes;  // x0, x1 and dZ segments of one chunk
 };
 
-// Warps 0-7 stage chunks; warp 8 issues the MMAs.  full[b] (8 warp
-// arrivals) hands a staged buffer to the MMA warp, empty[b] (its commit)
-// hands it back; done (a commit after a pass's last chunk) hands the
-// accumulators to warps 0-7 for the read-out.
+// Warp roles: warp 9 lane 0 fetches each chunk's raw rows with TMA (the
+// 66-pixel x segment of every input source, the 64-pixel dZ segment; out of
+// image pixels and rows arrive as zeros) into one of two raw buffers; warps
+// 0-7 transpose a raw buffer into one of two operand buffers; warp 8 lane 0
+// issues the MMAs.  Barriers: rawfull (TMA bytes), rawempty (8 warps done
+// reading), full (8 warps done writing), empty (MMA commit), done (a pass's
+// last commit, before the accumulator read-out).
 constexpr int kStageWarps = 8;
+constexpr int kXBox = kChunkPix + 2;  // x0 - 1 .. x0 + 64
+constexpr int kWgAllThreads = kWgThreads + 64;
 
-__global__ void __launch_bounds__(kWgThreads + 32, 1) k_wgrad_tc(const WgParams P) {
+__global__ void __launch_bounds__(kWgAllThreads, 1)
+    k_wgrad_tc(const __grid_constant__ CUtensorMap tx0, const __grid_constant__ CUtensorMap tx1,
+               const __grid_constant__ CUtensorMap tdz, const WgParams P) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ uint64_t full[2], empty[2], done;
+    __shared__ uint64_t full[2], empty[2], rawfull[2], rawempty[2], done;
     __shared__ uint32_t tmem_slot;
     __shared__ int s_ok;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int cin = P.c0 + P.c1, cout = P.cout;
     const int b_lbo = (cout / 8) * 128;
     const uint32_t b_off = 3u * kABytes;
+    const uint32_t raw0 = 2u * P.buf_bytes;  // raw buffers after the operand buffers
+    // TMA destinations start on 128-byte boundaries
+    const uint32_t x1_off = (uint32_t)(kXBox * P.c0 * 2 + 127) / 128 * 128;
+    const uint32_t dz_off = x1_off + (uint32_t)(kXBox * P.c1 * 2 + 127) / 128 * 128;
+    const uint32_t raw_tx = (uint32_t)(kXBox * cin * 2 + kChunkPix * cout * 2);
 
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
             umma::mbar_init(&full[b], kStageWarps);
             umma::mbar_init(&empty[b], 1);
+            umma::mbar_init(&rawfull[b], 1);
+            umma::mbar_init(&rawempty[b], kStageWarps);
         }
         umma::mbar_init(&done, 1);
         umma::mbar_init_fence();
         s_ok = 1;
     }
-    // A rows >= cin stay zero for the whole kernel
-    for (uint32_t i = tid * 16; i < 2 * P.buf_bytes; i += (kWgThreads + 32) * 16)
+    // operand rows >= cin stay zero for the whole kernel
+    for (uint32_t i = tid * 16; i < 2 * P.buf_bytes; i += kWgAllThreads * 16)
         *reinterpret_cast<uint4*>(smem + i) = make_uint4(0, 0, 0, 0);
     if (warp == kStageWarps) umma::tmem_alloc(&tmem_slot, P.tmem_cols);
     umma::fence_smem_to_async();
@@ -129,13 +146,32 @@ __global__ void __launch_bounds__(kWgThreads + 32, 1) k_wgrad_tc(const WgParams 
     const int per = (P.n_chunks + gridDim.x - 1) / gridDim.x;
     const int ch0 = blockIdx.x * per;
     const int ch1 = min(ch0 + per, P.n_chunks);
-    uint32_t fills[2] = {0, 0};  // chunks staged into each buffer so far (all passes)
+    uint32_t fills[2] = {0, 0};  // operand buffer uses (staging warps / MMA warp)
+    uint32_t raws[2] = {0, 0};   // raw buffer uses (producer / staging warps)
     uint32_t done_phase = 0;
     bool ok = true;
 
     for (int pass = 0; pass < 3 && ch0 < ch1; ++pass) {
         const int dy = pass - 1;
-        if (warp == kStageWarps) {
+        if (warp == kStageWarps + 1) {
+            if (lane == 0 && ok) {
+                int it = 0;
+                for (int ch = ch0; ch < ch1 && ok; ++ch, ++it) {
+                    const int rb = it & 1;
+                    if (raws[rb] > 0) ok = umma::mbar_wait(&rawempty[rb], (raws[rb] - 1) & 1u);
+                    if (!ok) break;
+                    const int row = ch / P.cpr, x0 = (ch - row * P.cpr) * kChunkPix;
+                    const int y = row % P.H, b = row / P.H;
+                    unsigned char* r = smem + raw0 + (uint32_t)rb * P.raw_bytes;
+                    umma::mbar_arrive_expect_tx(&rawfull[rb], raw_tx);
+                    umma::tma_load_4d(r, &tx0, 0, x0 - 1, y + dy, b, &rawfull[rb]);
+                    if (P.c1) umma::tma_load_4d(r + x1_off, &tx1, 0, x0 - 1, y + dy, b, &rawfull[rb]);
+                    umma::tma_load_4d(r + dz_off, &tdz, 0, x0, y, b, &rawfull[rb]);
+                    ++raws[rb];
+                }
+                if (!ok) s_ok = 0;
+            }
+        } else if (warp == kStageWarps) {
             if (lane == 0 && ok) {
                 const uint32_t idesc = umma::idesc_bf16_f32(kRowsA, cout);
                 const uint64_t a_desc = umma::smem_desc(umma::smem_u32(smem), kALbo, 128);
@@ -164,65 +200,60 @@ __global__ void __launch_bounds__(kWgThreads + 32, 1) k_wgrad_tc(const WgParams 
                 umma::commit(&done);
                 if (!ok) s_ok = 0;
             }
-            // fills[] of lane 0 is the only copy the MMA warp uses
         } else {
+            const int cz8 = cout / 8, ci8 = cin / 8, c08 = P.c0 / 8;
             int it = 0;
             for (int ch = ch0; ch < ch1; ++ch, ++it) {
                 const int buf = it & 1;
                 unsigned char* base = smem + (uint32_t)buf * P.buf_bytes;
-                // the MMAs that read this buffer's previous chunk must be done
-                if (fills[buf] > 0) {
-                    bool w = true;
-                    if (lane == 0) w = umma::mbar_wait(&empty[buf], (fills[buf] - 1) & 1u);
-                    w = __shfl_sync(0xffffffffu, w ? 1 : 0, 0) != 0;
-                    if (!w) {
-                        ok = false;
-                        break;
-                    }
+                const unsigned char* r = smem + raw0 + (uint32_t)buf * P.raw_bytes;
+                bool w = true;
+                if (lane == 0) {
+                    w = umma::mbar_wait(&rawfull[buf], raws[buf] & 1u);
+                    // the MMAs that read this operand buffer's previous chunk must be done
+                    if (w && fills[buf] > 0) w = umma::mbar_wait(&empty[buf], (fills[buf] - 1) & 1u);
                 }
-                // this chunk: pixels x0 .. x0 + 63 of image row `row` (= b * H + y)
-                const int row = ch / P.cpr, x0 = (ch - row * P.cpr) * kChunkPix;
-                const int y = row % P.H;
-                // stage B = dZ^T: a lane group of 8 loads 8 pixels' 8-channel
-                // groups and transposes them into 8 rows of 8 pixels
-                const int cz8 = cout / 8;
+                w = __shfl_sync(0xffffffffu, w ? 1 : 0, 0) != 0;
+                if (!w) {
+                    ok = false;
+                    break;
+                }
+                // B = dZ^T: a lane group of 8 reads 8 pixels' 8-channel groups
+                // and transposes them into 8 rows of 8 pixels
                 for (int i = tid; i < kChunkPix * cz8; i += kWgThreads) {  // multiple of 32
                     const int kk = i & 7, rest = i >> 3;
                     const int g = rest % cz8, kg = rest / cz8;
-                    const int x = x0 + 8 * kg + kk;
-                    uint4 u = make_uint4(0, 0, 0, 0);
-                    if (x < P.W)
-                        u = *reinterpret_cast<const uint4*>(P.dz + ((size_t)row * P.W + x) * cout + 8 * g);
-                    uint32_t w[4] = {u.x, u.y, u.z, u.w};
-                    transpose8(w, kk);
+                    const uint4 u = *reinterpret_cast<const uint4*>(
+                        r + dz_off + (uint32_t)(((8 * kg + kk) * cout + 8 * g) * 2));
+                    uint32_t wv[4] = {u.x, u.y, u.z, u.w};
+                    transpose8(wv, kk);
                     *reinterpret_cast<uint4*>(base + b_off + (uint32_t)(g * 128 + kg * b_lbo + kk * 16)) =
-                        make_uint4(w[0], w[1], w[2], w[3]);
+                        make_uint4(wv[0], wv[1], wv[2], wv[3]);
                 }
-                // stage A_dx = X shifted by (dy, dx), dx = -1, 0, 1, the same way
-                const int ci8 = cin / 8, c08 = P.c0 / 8;
-                const bool row_in = y + dy >= 0 && y + dy < P.H;
-                const size_t src_row = (size_t)(row + dy) * P.W;
+                // A_dx = X shifted by (dy, dx): pixel k + dx of the 66-pixel segment
                 for (int i = tid; i < 3 * kChunkPix * ci8; i += kWgThreads) {  // multiple of 32
                     const int kk = i & 7, rest = i >> 3;
                     const int g = rest % ci8, rest2 = rest / ci8;
                     const int kg = rest2 & 7, dxi = rest2 >> 3;
-                    const int x = x0 + 8 * kg + kk, sx = x + dxi - 1;
-                    uint4 u = make_uint4(0, 0, 0, 0);
-                    if (row_in && x < P.W && sx >= 0 && sx < P.W) {
-                        const size_t src = src_row + sx;
-                        u = g < c08 ? *reinterpret_cast<const uint4*>(P.x0 + src * P.c0 + 8 * g)
-                                    : *reinterpret_cast<const uint4*>(P.x1 + src * P.c1 + 8 * (g - c08));
-                    }
-                    uint32_t w[4] = {u.x, u.y, u.z, u.w};
-                    transpose8(w, kk);
+                    const int px = 8 * kg + kk + dxi;
+                    const uint4 u = g < c08
+                        ? *reinterpret_cast<const uint4*>(r + (uint32_t)((px * P.c0 + 8 * g) * 2))
+                        : *reinterpret_cast<const uint4*>(r + x1_off +
+                                                          (uint32_t)((px * P.c1 + 8 * (g - c08)) * 2));
+                    uint32_t wv[4] = {u.x, u.y, u.z, u.w};
+                    transpose8(wv, kk);
                     *reinterpret_cast<uint4*>(base + (uint32_t)dxi * kABytes +
                                               (uint32_t)(g * 128 + kg * kALbo + kk * 16)) =
-                        make_uint4(w[0], w[1], w[2], w[3]);
+                        make_uint4(wv[0], wv[1], wv[2], wv[3]);
                 }
                 umma::fence_smem_to_async();
                 __syncwarp();
-                if (lane == 0) umma::mbar_arrive(&full[buf]);
+                if (lane == 0) {
+                    umma::mbar_arrive(&rawempty[buf]);
+                    umma::mbar_arrive(&full[buf]);
+                }
                 ++fills[buf];
+                ++raws[buf];
             }
         }
         // the pass's accumulators: wait for the last commit, then read
@@ -252,8 +283,7 @@ __global__ void __launch_bounds__(kWgThreads + 32, 1) k_wgrad_tc(const WgParams 
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const int col = c + j, dxi = col / cout, co = col % cout;
-                        const int t = (dy + 1) * 3 + dxi;
-                        atomicAdd(P.dw + ((size_t)co * cin + ci) * 9 + t, v[j]);
+                        atomicAdd(P.dw + ((size_t)co * cin + ci) * 9 + (dy + 1) * 3 + dxi, v[j]);
                     }
                 }
             }
@@ -262,8 +292,7 @@ __global__ void __launch_bounds__(kWgThreads + 32, 1) k_wgrad_tc(const WgParams 
         __syncthreads();
         umma::fence_after_sync();
     }
-    if (!ok && tid == 0) atomicOr(P.status, 4);
-    if (tid == 0 && !s_ok) atomicOr(P.status, 4);
+    if (tid == 0 && (!ok || !s_ok)) atomicOr(P.status, 4);
     umma::fence_before_sync();
     __syncthreads();
     if (warp == kStageWarps) umma::tmem_dealloc(tmem, P.tmem_cols);
@@ -295,6 +324,33 @@ __global__ void __launch_bounds__(256) k_bias_grad(const uint16_t* __restrict__ 
 }
 
 int wg_fail(int code, const char* msg) { return set_last_error(code, msg); }
+
+PFN_cuTensorMapEncodeTiled_v12000 wg_encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 4-D map of an NHWC bf16 tensor whose box is one row segment: {all C
+// channels, box_w pixels, 1 row, 1 image} (C * 2 bytes <= 256 elements' worth)
+bool encode_rows(CUtensorMap* map, const void* base, int B, int H, int W, int C, int box_w) {
+    auto fn = wg_encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    cuuint32_t box[4] = {(cuuint32_t)C, (cuuint32_t)box_w, 1, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box,
+              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 // status word of the weight-gradient kernels (bit 2: a bounded wait ran out)
 __device__ int g_wgrad_status;
@@ -330,19 +386,23 @@ int wgrad_tc(const uint16_t* dz, int cout, const uint16_t* x0, int c0, const uin
     while (cols < (uint32_t)(3 * cout)) cols *= 2;
     P.tmem_cols = cols;
     P.buf_bytes = 3u * kABytes + (uint32_t)cout * kChunkPix * 2u;
-    const uint32_t smem = 2u * P.buf_bytes;
-    static bool attr = false;
-    if (!attr) {
-        if (cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 2 * (3 * kABytes + kBMaxBytes)) != cudaSuccess)
-            return wg_fail(NATRIX_ECUDA, "wgrad: shared memory attribute");
-        attr = true;
-    }
+    P.raw_bytes = (uint32_t)(kXBox * c0 * 2 + 127) / 128 * 128 +
+                  (uint32_t)(kXBox * c1 * 2 + 127) / 128 * 128 + (uint32_t)kChunkPix * cout * 2u;
+    P.raw_bytes = (P.raw_bytes + 127u) / 128u * 128u;
+    const uint32_t smem = 2u * P.buf_bytes + 2u * P.raw_bytes;
+    CUtensorMap tx0, tx1, tdz;
+    if (!encode_rows(&tx0, x0, B, H, W, c0, kXBox) ||
+        !encode_rows(&tx1, c1 ? x1 : x0, B, H, W, c1 ? c1 : c0, kXBox) ||
+        !encode_rows(&tdz, dz, B, H, W, cout, kChunkPix))
+        return wg_fail(NATRIX_ECUDA, "wgrad: tensor map encoding failed");
+    if (cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return wg_fail(NATRIX_ECUDA, "wgrad: shared memory attribute");
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int grid = P.n_chunks < sms ? P.n_chunks : sms;
-    k_wgrad_tc<<<grid, kWgThreads + 32, smem, st>>>(P);
+    k_wgrad_tc<<<grid, kWgAllThreads, smem, st>>>(tx0, tx1, tdz, P);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return wg_fail(NATRIX_ECUDA, cudaGetErrorString(e));
     if (db) {
