@@ -52,6 +52,9 @@ __device__ __forceinline__ bool disc_meets_box(float cx, float cy, float r, int 
     return dx * dx + dy * dy <= rr * rr;
 }
 
+// ROWS: rows of cells per thread (the block covers BX x BY*ROWS cells, the
+// shape list is loaded and culled once for all of them).
+template <int ROWS = 1>
 __device__ __forceinline__ void block_obstacles(uint8_t* __restrict__ mask, Grid g,
                                                 const ShapeOp* __restrict__ ops, int n, int fresh,
                                                 int bx0, int by0) {
@@ -60,7 +63,7 @@ __device__ __forceinline__ void block_obstacles(uint8_t* __restrict__ mask, Grid
     const int tid = threadIdx.y * BX + threadIdx.x;
     for (int i = tid; i < n; i += BX * BY) s_ops[i] = ops[i];
     __syncthreads();
-    const int bx1 = bx0 + BX - 1, by1 = by0 + BY - 1;
+    const int bx1 = bx0 + BX - 1, by1 = by0 + BY * ROWS - 1;
     const int nk = cull_ops(n, s_kept, [&](int k) {
         const ShapeOp& op = s_ops[k];
         // triangles are never culled: the reference's same-sign test marks
@@ -69,26 +72,31 @@ __device__ __forceinline__ void block_obstacles(uint8_t* __restrict__ mask, Grid
         return disc_meets_box(op.a[0] * (float)g.W, op.a[1] * (float)g.H, op.a[2], bx0, bx1,
                               by0, by1);
     });
-    const int x = bx0 + threadIdx.x, y = by0 + threadIdx.y;
-    if (x >= g.W || y >= g.H) return;
-    const size_t i = (size_t)y * g.P + x;
     if (nk == 0 && !fresh) return;
-    uint8_t m = fresh ? 0 : mask[i];
-    for (int kk = 0; kk < nk; ++kk) {
-        const ShapeOp& op = s_ops[s_kept[kk]];
-        if (op.kind == SHAPE_CIRCLE) {
-            const float spx = op.a[0] * (float)g.W, spy = op.a[1] * (float)g.H;
-            const float dx = spx - (float)x, dy = spy - (float)y;
-            if (sqrtf(dx * dx + dy * dy) <= op.a[2]) m = 1;  // vec2(1, 0), both branches
-        } else {
-            const float ptx = (float)x / (float)g.W, pty = (float)y / (float)g.H;
-            const bool b1 = tri_sign(ptx, pty, op.a[0], op.a[1], op.a[2], op.a[3]) < 0.0f;
-            const bool b2 = tri_sign(ptx, pty, op.a[2], op.a[3], op.a[4], op.a[5]) < 0.0f;
-            const bool b3 = tri_sign(ptx, pty, op.a[4], op.a[5], op.a[0], op.a[1]) < 0.0f;
-            if (b1 == b2 && b2 == b3) m = (uint8_t)((m & ~3) | (op.is_static ? 2 : 1));
+    const int x = bx0 + threadIdx.x;
+    if (x >= g.W) return;
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        const int y = by0 + threadIdx.y + r * BY;
+        if (y >= g.H) break;
+        const size_t i = (size_t)y * g.P + x;
+        uint8_t m = fresh ? 0 : mask[i];
+        for (int kk = 0; kk < nk; ++kk) {
+            const ShapeOp& op = s_ops[s_kept[kk]];
+            if (op.kind == SHAPE_CIRCLE) {
+                const float spx = op.a[0] * (float)g.W, spy = op.a[1] * (float)g.H;
+                const float dx = spx - (float)x, dy = spy - (float)y;
+                if (sqrtf(dx * dx + dy * dy) <= op.a[2]) m = 1;  // vec2(1, 0), both branches
+            } else {
+                const float ptx = (float)x / (float)g.W, pty = (float)y / (float)g.H;
+                const bool b1 = tri_sign(ptx, pty, op.a[0], op.a[1], op.a[2], op.a[3]) < 0.0f;
+                const bool b2 = tri_sign(ptx, pty, op.a[2], op.a[3], op.a[4], op.a[5]) < 0.0f;
+                const bool b3 = tri_sign(ptx, pty, op.a[4], op.a[5], op.a[0], op.a[1]) < 0.0f;
+                if (b1 == b2 && b2 == b3) m = (uint8_t)((m & ~3) | (op.is_static ? 2 : 1));
+            }
         }
+        mask[i] = m;
     }
-    mask[i] = m;
 }
 
 // ------------------------------------------------------------------ forcing
@@ -109,6 +117,7 @@ __device__ __forceinline__ bool op_is_velocity(int kind) {
     return kind == FORCE_CONE_VELOCITY || kind == FORCE_GAUSS;
 }
 
+template <int ROWS = 1>
 __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
                                               float* __restrict__ rho, Grid gd,
                                               const ForceOp* __restrict__ ops, int n, int bx0,
@@ -118,8 +127,8 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
     const int tid = threadIdx.y * BX + threadIdx.x;
     for (int i = tid; i < n; i += BX * BY) s_ops[i] = ops[i];
     __syncthreads();
-    const int bx1 = bx0 + BX - 1, by1 = by0 + BY - 1;
-    const int x = bx0 + threadIdx.x, y = by0 + threadIdx.y;
+    const int bx1 = bx0 + BX - 1, by1 = by0 + BY * ROWS - 1;
+    const int x = bx0 + threadIdx.x;
     if (vel) {
         int first_vel = -1;
         for (int k = 0; k < n; ++k)
@@ -137,7 +146,10 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
                                       bx1, by0, by1);
             return false;
         });
-        if (first_vel >= 0 && x < gv.W && y < gv.H) {
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            const int y = by0 + threadIdx.y + r * BY;
+            if (first_vel < 0 || x >= gv.W || y >= gv.H) continue;
             const size_t i = (size_t)y * gv.P + x;
             float2 a = vel[i];
             // the first velocity op culled for this block: it clamps the cell
@@ -191,7 +203,10 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
                                                        op.r, bx0, bx1, by0, by1);
             return false;
         });
-        if (nk > 0 && x < gd.W && y < gd.H) {
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            const int y = by0 + threadIdx.y + r * BY;
+            if (nk == 0 || x >= gd.W || y >= gd.H) continue;
             const size_t i = (size_t)y * gd.P + x;
             float a = rho[i];
             for (int kk = 0; kk < nk; ++kk) {

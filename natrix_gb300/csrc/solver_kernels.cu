@@ -30,16 +30,22 @@ inline dim3 grid_cpt(const Grid& g) {
         }                                                            \
     } while (0)
 
+// Forcing and obstacles: FORCE_ROWS rows of cells per thread, so the op list
+// is loaded and culled once per BX x (BY * FORCE_ROWS) cells.
+constexpr int FORCE_ROWS = 4;
+
 __global__ void __launch_bounds__(BX* BY)
     k_obstacles(uint8_t* __restrict__ mask, Grid g, const ShapeOp* __restrict__ ops, int n,
                 int fresh) {
-    block_obstacles(mask, g, ops, n, fresh, blockIdx.x * BX, blockIdx.y * BY);
+    block_obstacles<FORCE_ROWS>(mask, g, ops, n, fresh, blockIdx.x * BX,
+                                blockIdx.y * BY * FORCE_ROWS);
 }
 
 __global__ void __launch_bounds__(BX* BY)
     k_forcing(float2* __restrict__ vel, Grid gv, float* __restrict__ rho, Grid gd,
               const ForceOp* __restrict__ ops, int n) {
-    block_forcing(vel, gv, rho, gd, ops, n, blockIdx.x * BX, blockIdx.y * BY);
+    block_forcing<FORCE_ROWS>(vel, gv, rho, gd, ops, n, blockIdx.x * BX,
+                              blockIdx.y * BY * FORCE_ROWS);
 }
 
 __global__ void __launch_bounds__(BX* BY) k_advect(const float2* __restrict__ vin, float2* __restrict__ vout,
@@ -423,7 +429,8 @@ cudaError_t launch_residual_labels(const float* p, const float* div, const uint8
 
 cudaError_t launch_obstacles(uint8_t* mask, Grid g, const ShapeOp* ops, int n, int fresh,
                              cudaStream_t st) {
-    k_obstacles<<<grid_for(g), dim3(BX, BY), 0, st>>>(mask, g, ops, n, fresh);
+    k_obstacles<<<dim3((g.W + BX - 1) / BX, (g.H + BY * FORCE_ROWS - 1) / (BY * FORCE_ROWS)),
+                  dim3(BX, BY), 0, st>>>(mask, g, ops, n, fresh);
     return cudaGetLastError();
 }
 
@@ -431,7 +438,8 @@ cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const Forc
                            int n, cudaStream_t st) {
     Grid gg = vel ? gv : gd;
     if (vel && rho) gg = Grid{gv.W > gd.W ? gv.W : gd.W, gv.H > gd.H ? gv.H : gd.H, 0};
-    k_forcing<<<grid_for(gg), dim3(BX, BY), 0, st>>>(vel, gv, rho, gd, ops, n);
+    k_forcing<<<dim3((gg.W + BX - 1) / BX, (gg.H + BY * FORCE_ROWS - 1) / (BY * FORCE_ROWS)),
+                dim3(BX, BY), 0, st>>>(vel, gv, rho, gd, ops, n);
     return cudaGetLastError();
 }
 
