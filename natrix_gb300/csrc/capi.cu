@@ -79,44 +79,6 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
-// Pinned staging for host -> device copies of op lists and step parameters.
-// Each slot is reused only after the copy that last read it has completed.
-struct UploadRing {
-    static constexpr int kSlots = 8;
-    static constexpr size_t kSlotBytes = 16 * 1024;  // >= 256 ops of 32 bytes
-    unsigned char* host = nullptr;
-    cudaEvent_t ev[kSlots] = {};
-    int next = 0;
-
-    cudaError_t init() {
-        cudaError_t e = cudaMallocHost(&host, kSlots * kSlotBytes);
-        if (e != cudaSuccess) return e;
-        for (int i = 0; i < kSlots; ++i) {
-            e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
-            if (e != cudaSuccess) return e;
-        }
-        return cudaSuccess;
-    }
-    void release() {
-        for (int i = 0; i < kSlots; ++i)
-            if (ev[i]) cudaEventDestroy(ev[i]);
-        if (host) cudaFreeHost(host);
-        host = nullptr;
-    }
-    cudaError_t upload(void* dev, const void* src, size_t n, cudaStream_t st) {
-        if (n > kSlotBytes) return cudaErrorInvalidValue;
-        const int s = next;
-        next = (next + 1) % kSlots;
-        cudaError_t e = cudaEventSynchronize(ev[s]);
-        if (e != cudaSuccess) return e;
-        unsigned char* slot = host + (size_t)s * kSlotBytes;
-        std::memcpy(slot, src, n);
-        e = cudaMemcpyAsync(dev, slot, n, cudaMemcpyHostToDevice, st);
-        if (e != cudaSuccess) return e;
-        return cudaEventRecord(ev[s], st);
-    }
-};
-
 }  // namespace
 
 struct natrix_sim {
@@ -130,16 +92,12 @@ struct natrix_sim {
     uint8_t* mask = nullptr;
     uint8_t* flags = nullptr;
     int p_cur = 0;
-    StepParams* d_sp = nullptr;
-    ForceOp* d_force = nullptr;
-    ShapeOp* d_shape = nullptr;
     int* d_status = nullptr;
     double* d_res = nullptr;  // partials, then the 5 sums at the end
     double* h_res = nullptr;  // pinned
     int res_blocks = 0;
     JacobiMaps maps{};             // host copy (encoded at creation)
     JacobiMaps* d_maps = nullptr;  // device copy the sweep kernels read
-    UploadRing ring;
     std::vector<ForceOp> fq;
     std::vector<ShapeOp> sq;
     bool mask_reset_pending = true;  // the mask memory does not hold the current obstacles
@@ -160,9 +118,6 @@ struct natrix_density {
     float speed = 500.0f;
     float dissipation = 1.0f;
     int simulate = 1;
-    StepParams* d_sp = nullptr;
-    ForceOp* d_force = nullptr;
-    UploadRing ring;
     std::vector<ForceOp> fq;
 };
 
@@ -187,14 +142,10 @@ void free_sim(natrix_sim* s) {
     cudaFree(s->vort);
     cudaFree(s->mask);
     cudaFree(s->flags);
-    cudaFree(s->d_sp);
-    cudaFree(s->d_force);
-    cudaFree(s->d_shape);
     cudaFree(s->d_status);
     cudaFree(s->d_res);
     cudaFree(s->d_maps);
     if (s->h_res) cudaFreeHost(s->h_res);
-    s->ring.release();
     delete s;
 }
 
@@ -228,8 +179,7 @@ int flush_shapes(natrix_sim* s, cudaStream_t st) {
     size_t done = 0;
     while (done < s->sq.size()) {
         const int n = (int)std::min<size_t>(kMaxOpsPerLaunch, s->sq.size() - done);
-        NX_CUDA(s->ring.upload(s->d_shape, s->sq.data() + done, n * sizeof(ShapeOp), st));
-        NX_LAUNCH(s, launch_obstacles(s->mask, s->g, s->d_shape, n,
+        NX_LAUNCH(s, launch_obstacles(s->mask, s->g, s->sq.data() + done, n,
                                       s->mask_reset_pending ? 1 : 0, st));
         s->mask_reset_pending = false;
         done += n;
@@ -238,13 +188,12 @@ int flush_shapes(natrix_sim* s, cudaStream_t st) {
     return NATRIX_OK;
 }
 
-int flush_force_list(natrix_sim* s, UploadRing& ring, ForceOp* d_ops, std::vector<ForceOp>& q,
-                     float2* vel, Grid gv, float* rho, Grid gd, cudaStream_t st) {
+int flush_force_list(natrix_sim* s, std::vector<ForceOp>& q, float2* vel, Grid gv, float* rho,
+                     Grid gd, cudaStream_t st) {
     size_t done = 0;
     while (done < q.size()) {
         const int n = (int)std::min<size_t>(kMaxOpsPerLaunch, q.size() - done);
-        NX_CUDA(ring.upload(d_ops, q.data() + done, n * sizeof(ForceOp), st));
-        NX_LAUNCH(s, launch_forcing(vel, gv, rho, gd, d_ops, n, st));
+        NX_LAUNCH(s, launch_forcing(vel, gv, rho, gd, q.data() + done, n, st));
         done += n;
     }
     q.clear();
@@ -254,12 +203,11 @@ int flush_force_list(natrix_sim* s, UploadRing& ring, ForceOp* d_ops, std::vecto
 int flush_fluid(natrix_sim* s, cudaStream_t st) {
     int rc = flush_shapes(s, st);
     if (rc) return rc;
-    return flush_force_list(s, s->ring, s->d_force, s->fq, s->vel[0], s->g, nullptr, Grid{}, st);
+    return flush_force_list(s, s->fq, s->vel[0], s->g, nullptr, Grid{}, st);
 }
 
 int flush_density(natrix_density* d, cudaStream_t st) {
-    return flush_force_list(d->fluid, d->ring, d->d_force, d->fq, nullptr, Grid{}, d->rho[d->cur],
-                            d->g, st);
+    return flush_force_list(d->fluid, d->fq, nullptr, Grid{}, d->rho[d->cur], d->g, st);
 }
 
 int run_jacobi(natrix_sim* s, int sweeps, cudaStream_t st) {
@@ -379,14 +327,10 @@ int natrix_create(int32_t width, int32_t height, natrix_sim** out) {
     if (e == cudaSuccess) e = alloc((void**)&s->vort, cells * 4);
     if (e == cudaSuccess) e = alloc((void**)&s->mask, cells);
     if (e == cudaSuccess) e = alloc((void**)&s->flags, cells);
-    if (e == cudaSuccess) e = alloc((void**)&s->d_sp, sizeof(StepParams));
-    if (e == cudaSuccess) e = alloc((void**)&s->d_force, kMaxOpsPerLaunch * sizeof(ForceOp));
-    if (e == cudaSuccess) e = alloc((void**)&s->d_shape, kMaxOpsPerLaunch * sizeof(ShapeOp));
     if (e == cudaSuccess) e = alloc((void**)&s->d_status, sizeof(int));
     s->res_blocks = residual_partials(s->g);
     if (e == cudaSuccess) e = alloc((void**)&s->d_res, ((size_t)s->res_blocks + 1) * 5 * 8);
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_res, 5 * sizeof(double));
-    if (e == cudaSuccess) e = s->ring.init();
     if (e != cudaSuccess) {
         free_sim(s);
         return fail(e == cudaErrorMemoryAllocation ? NATRIX_ENOMEM : NATRIX_ECUDA,
@@ -487,20 +431,19 @@ int natrix_step(natrix_sim* s, float dt, void* stream) {
     if (rc) return rc;
     const bool mask_zero = s->mask_reset_pending;
     const StepParams sp = fluid_params(s, dt, mask_zero);
-    NX_CUDA(s->ring.upload(s->d_sp, &sp, sizeof sp, st));
 
     const Grid g = s->g;
-    NX_LAUNCH(s, launch_advect(s->vel[0], s->vel[1], s->mask, g, s->d_sp, st));
+    NX_LAUNCH(s, launch_advect(s->vel[0], s->vel[1], s->mask, g, sp, st));
     int cur = 1;
     if (s->prm.vorticity > 0.0f) {
-        NX_LAUNCH(s, launch_vorticity(s->vel[cur], s->vel[3 - cur], s->vort, g, s->d_sp, st));
+        NX_LAUNCH(s, launch_vorticity(s->vel[cur], s->vel[3 - cur], s->vort, g, sp, st));
         cur = 3 - cur;
     }
     if (s->prm.viscosity > 0.0f) {
-        NX_LAUNCH(s, launch_viscosity(s->vel[cur], s->vel[3 - cur], g, s->d_sp, st));
+        NX_LAUNCH(s, launch_viscosity(s->vel[cur], s->vel[3 - cur], g, sp, st));
         cur = 3 - cur;
     }
-    NX_LAUNCH(s, launch_divergence(s->vel[cur], s->mask, s->div, s->flags, s->p[0], g, s->d_sp, st));
+    NX_LAUNCH(s, launch_divergence(s->vel[cur], s->mask, s->div, s->flags, s->p[0], g, sp, st));
     s->p_cur = 0;
     rc = run_jacobi(s, s->prm.iterations - 1, st);
     if (rc) return rc;
@@ -525,9 +468,8 @@ int natrix_residual(natrix_sim* s, double out[5], void* stream) {
     cudaStream_t st = stream_of(s, stream);
     // the obstacles the last step's sweeps used
     const StepParams sp = fluid_params(s, 0.0f, s->last_step_mask_zero);
-    NX_CUDA(s->ring.upload(s->d_sp, &sp, sizeof sp, st));
     double* sums = s->d_res + (size_t)s->res_blocks * 5;
-    NX_CUDA(launch_residual(s->p[s->p_cur], s->div, s->mask, s->flags, s->g, s->d_sp, s->d_res,
+    NX_CUDA(launch_residual(s->p[s->p_cur], s->div, s->mask, s->flags, s->g, sp, s->d_res,
                             sums, st));
     s->stats.kernel_launches += 2;
     NX_CUDA(cudaMemcpyAsync(s->h_res, sums, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -648,9 +590,6 @@ int natrix_density_create(natrix_sim* fluid, int32_t width, int32_t height,
     if (e == cudaSuccess) e = cudaMemset(d->rho[0], 0, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&d->rho[1], bytes);
     if (e == cudaSuccess) e = cudaMemset(d->rho[1], 0, bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&d->d_sp, sizeof(StepParams));
-    if (e == cudaSuccess) e = cudaMalloc(&d->d_force, kMaxOpsPerLaunch * sizeof(ForceOp));
-    if (e == cudaSuccess) e = d->ring.init();
     if (e != cudaSuccess) {
         natrix_density_destroy(d);
         return fail(NATRIX_ENOMEM, "allocating a %dx%d density grid: %s", width, height,
@@ -665,9 +604,6 @@ int natrix_density_destroy(natrix_density* d) {
     cudaDeviceSynchronize();
     cudaFree(d->rho[0]);
     cudaFree(d->rho[1]);
-    cudaFree(d->d_sp);
-    cudaFree(d->d_force);
-    d->ring.release();
     delete d;
     return NATRIX_OK;
 }
@@ -706,9 +642,8 @@ int natrix_density_step(natrix_density* d, float dt, void* stream) {
     StepParams sp = fluid_params(s, dt, s->mask_reset_pending);
     sp.d_speed = d->speed;
     sp.d_dissipation = d->dissipation;
-    NX_CUDA(d->ring.upload(d->d_sp, &sp, sizeof sp, st));
     NX_LAUNCH(s, launch_density_advect(d->rho[d->cur], d->rho[1 - d->cur], d->g, s->vel[0], s->mask,
-                                  s->g, d->d_sp, st));
+                                  s->g, sp, st));
     d->cur ^= 1;
     return NATRIX_OK;
 }

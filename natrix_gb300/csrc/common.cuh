@@ -98,4 +98,38 @@ __device__ __forceinline__ float nx_expf(float x) {
 // beyond a wall, where the clamped index of common.sh:9-19 is the cell itself.
 enum : uint8_t { NB_L = 1, NB_R = 2, NB_B = 4, NB_T = 8 };
 
+// Programmatic dependent launch.  The kernels of the single-grid step are
+// launched with programmatic stream serialisation, so a launch is scheduled
+// while its predecessor on the stream drains instead of after it has retired.
+// Every block calls pdl_enter() before anything else: it allows the next
+// launch to be scheduled, then waits until the predecessor grid has completed
+// and its writes are visible.  (The next launch cannot get ahead either: its
+// own pdl_enter() waits for this grid, which finishes only after this wait.)
+// In a kernel launched without the attribute both instructions do nothing.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// Whether step launches use programmatic dependent launch (on unless the
+// environment sets NATRIX_PDL=0).
+bool pdl_enabled();
+
+// Launch `kernel` on `st`, with programmatic stream serialisation if `pdl`.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_kernel(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                          cudaStream_t st, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 }  // namespace natrix

@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(C::THREADS_X* C::THREADS_Y)
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
     __shared__ int s_ok;
 
+    pdl_enter();
     const TileJob job = jobs(blockIdx.x);
     const int tile_x = job.tile_x, tile_y = job.tile_y, sweeps = job.sweeps;
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -286,6 +287,7 @@ __global__ void __launch_bounds__(C::THREADS, 1)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int c0 = lane * 4, r0 = w * R;
 
+    pdl_enter();
     int t = blockIdx.x;
     if (t >= jobs.n) return;
     if (threadIdx.x == 0) {
@@ -478,7 +480,7 @@ cudaError_t set_smem(K kernel, int bytes) {
 }
 
 template <class C, class Jobs>
-cudaError_t launch_rt_jobs(const Jobs& jobs, int* status, cudaStream_t st) {
+cudaError_t launch_rt_jobs(const Jobs& jobs, int* status, cudaStream_t st, bool pdl) {
     static bool attr = false;
     if (!attr) {
         cudaError_t e = set_smem(k_jacobi_rt<C, Jobs>, C::SMEM);
@@ -487,12 +489,12 @@ cudaError_t launch_rt_jobs(const Jobs& jobs, int* status, cudaStream_t st) {
     }
     if (jobs.n == 0) return cudaSuccess;
     const int grid = jobs.n < num_sms() ? jobs.n : num_sms();
-    k_jacobi_rt<C, Jobs><<<grid, C::THREADS, C::SMEM, st>>>(jobs, status);
-    return cudaGetLastError();
+    return launch_kernel(pdl, k_jacobi_rt<C, Jobs>, dim3(grid), dim3(C::THREADS), C::SMEM, st, jobs,
+                         status);
 }
 
 template <class C, class Jobs>
-cudaError_t launch_tb_jobs(const Jobs& jobs, int* status, cudaStream_t st) {
+cudaError_t launch_tb_jobs(const Jobs& jobs, int* status, cudaStream_t st, bool pdl) {
     static bool attr = false;
     if (!attr) {
         cudaError_t e = set_smem(k_jacobi_tb<C, Jobs>, C::SMEM);
@@ -500,8 +502,8 @@ cudaError_t launch_tb_jobs(const Jobs& jobs, int* status, cudaStream_t st) {
         attr = true;
     }
     if (jobs.n == 0) return cudaSuccess;
-    k_jacobi_tb<C, Jobs><<<jobs.n, dim3(C::THREADS_X, C::THREADS_Y), C::SMEM, st>>>(jobs, status);
-    return cudaGetLastError();
+    return launch_kernel(pdl, k_jacobi_tb<C, Jobs>, dim3(jobs.n), dim3(C::THREADS_X, C::THREADS_Y),
+                         C::SMEM, st, jobs, status);
 }
 
 template <class C>
@@ -554,17 +556,19 @@ cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbu
     const int tiles_x = (g.W + tx - 1) / tx, tiles_y = (g.H + ty - 1) / ty;
     const GridJobs jobs{&d_maps->p[src], &d_maps->div, &d_maps->flags, pbuf[1 - src], g,
                         sweeps, tiles_x, tiles_x * tiles_y, tx, ty};
-    if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st);
-    if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st);
-    return launch_tb_jobs<Tb>(jobs, status, st);
+    const bool pdl = pdl_enabled();
+    if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st, pdl);
+    if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st, pdl);
+    return launch_tb_jobs<Tb>(jobs, status, st, pdl);
 }
 
 cudaError_t launch_jacobi_batch(int config, const JacobiBatchItem* items, int n_items,
                                 const JacobiBatchSim* sims, int* status, cudaStream_t st) {
     const BatchJobs jobs{items, sims, n_items};
-    if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st);
-    if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st);
-    return launch_tb_jobs<Tb>(jobs, status, st);
+    // replayed from a CUDA graph: plain stream order
+    if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st, false);
+    if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st, false);
+    return launch_tb_jobs<Tb>(jobs, status, st, false);
 }
 
 }  // namespace natrix

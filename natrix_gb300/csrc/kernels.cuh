@@ -9,8 +9,9 @@
 
 namespace natrix {
 
-// Per-step scalars, resident in device memory so a captured CUDA graph can
-// replay a step with new values (the host copies a fresh block each step).
+// Per-step scalars.  The single-grid path passes them by value in each
+// launch's parameter block; the batch path keeps one block per simulation in
+// device memory, so its captured CUDA graph replays with new values.
 struct StepParams {
     float dt;
     float speed;
@@ -52,6 +53,13 @@ struct ShapeOp {
 // applies the ops in order).
 constexpr int kMaxOpsPerLaunch = 256;
 
+// An op list passed by value as a kernel parameter (at most CAP ops).
+template <typename Op, int CAP>
+struct OpBlock {
+    int n;
+    Op op[CAP];
+};
+
 // Record `msg` as the calling thread's natrix_last_error() and return `code`.
 int set_last_error(int code, const char* msg);
 
@@ -84,33 +92,34 @@ struct DeviceGuard {
 void sim_count_launches(natrix_sim* sim, int n);
 
 // ---- per-cell kernels (solver_kernels.cu) --------------------------------
+// `ops` is host memory (n <= kMaxOpsPerLaunch), copied into the launch.
 cudaError_t launch_obstacles(uint8_t* mask, Grid g, const ShapeOp* ops, int n, int fresh,
                              cudaStream_t st);
 cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const ForceOp* ops,
                            int n, cudaStream_t st);
 cudaError_t launch_advect(const float2* vin, float2* vout, const uint8_t* mask, Grid g,
-                          const StepParams* sp, cudaStream_t st);
+                          const StepParams& sp, cudaStream_t st);
 cudaError_t launch_calc_vorticity(const float2* v, float* w, Grid g, cudaStream_t st);
 // calc + apply in one pass (same results); writes the curl to w
 cudaError_t launch_vorticity(const float2* vin, float2* vout, float* w, Grid g,
-                             const StepParams* sp, cudaStream_t st);
+                             const StepParams& sp, cudaStream_t st);
 cudaError_t launch_apply_vorticity(const float2* vin, float2* vout, const float* w, Grid g,
-                                   const StepParams* sp, cudaStream_t st);
-cudaError_t launch_viscosity(const float2* vin, float2* vout, Grid g, const StepParams* sp,
+                                   const StepParams& sp, cudaStream_t st);
+cudaError_t launch_viscosity(const float2* vin, float2* vout, Grid g, const StepParams& sp,
                              cudaStream_t st);
 cudaError_t launch_divergence(const float2* v, const uint8_t* mask, float* div,
-                              uint8_t* flags, float* p1, Grid g, const StepParams* sp,
+                              uint8_t* flags, float* p1, Grid g, const StepParams& sp,
                               cudaStream_t st);
 cudaError_t launch_subtract_gradient(const float2* vin, float2* vout, const float* p,
                                      const uint8_t* flags, Grid g, cudaStream_t st);
 cudaError_t launch_density_advect(const float* rin, float* rout, Grid gd, const float2* v,
-                                  const uint8_t* mask, Grid gv, const StepParams* sp,
+                                  const uint8_t* mask, Grid gv, const StepParams& sp,
                                   cudaStream_t st);
 // Residual sums {n, sum r, sum r^2, sum b, sum b^2} into out[5] (device),
 // using `partials` (device, >= residual_partials(g) * 5 doubles).
 int residual_partials(Grid g);
 cudaError_t launch_residual(const float* p, const float* div, const uint8_t* mask,
-                            const uint8_t* flags, Grid g, const StepParams* sp,
+                            const uint8_t* flags, Grid g, const StepParams& sp,
                             double* partials, double* out, cudaStream_t st);
 
 // Per-region residual sums: labels dense W*H (fluid region id, < 0 for

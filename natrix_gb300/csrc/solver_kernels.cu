@@ -5,13 +5,13 @@
 // One thread per cell, 32x8 blocks (a warp spans 32 consecutive cells of a
 // row, so float2 velocity loads and stores coalesce into 256-byte segments).
 // Compiled with -fmad=false: see common.cuh for the arithmetic contract.
+#include <cstdlib>
+
 #include "cells.cuh"
 
 namespace natrix {
 
 namespace {
-
-inline dim3 grid_for(const Grid& g) { return dim3((g.W + BX - 1) / BX, (g.H + BY - 1) / BY); }
 
 // The streaming stencil kernels give each thread CPT cells of one column,
 // BY rows apart, so every thread has CPT independent load chains in flight
@@ -34,54 +34,80 @@ inline dim3 grid_cpt(const Grid& g) {
 // is loaded and culled once per BX x (BY * FORCE_ROWS) cells.
 constexpr int FORCE_ROWS = 4;
 
+// The op list travels in the launch's parameter block (no host-to-device
+// copy on the stream); CAP is the smallest of 16 / 64 / 256 that holds it.
+template <int CAP>
 __global__ void __launch_bounds__(BX* BY)
-    k_obstacles(uint8_t* __restrict__ mask, Grid g, const ShapeOp* __restrict__ ops, int n,
+    k_obstacles(uint8_t* __restrict__ mask, Grid g, const __grid_constant__ OpBlock<ShapeOp, CAP> ob,
                 int fresh) {
-    block_obstacles<FORCE_ROWS>(mask, g, ops, n, fresh, blockIdx.x * BX,
+    pdl_enter();
+    block_obstacles<FORCE_ROWS>(mask, g, ob.op, ob.n, fresh, blockIdx.x * BX,
                                 blockIdx.y * BY * FORCE_ROWS);
 }
 
+template <int CAP>
 __global__ void __launch_bounds__(BX* BY)
     k_forcing(float2* __restrict__ vel, Grid gv, float* __restrict__ rho, Grid gd,
-              const ForceOp* __restrict__ ops, int n) {
-    block_forcing<FORCE_ROWS>(vel, gv, rho, gd, ops, n, blockIdx.x * BX,
+              const __grid_constant__ OpBlock<ForceOp, CAP> ob) {
+    pdl_enter();
+    block_forcing<FORCE_ROWS>(vel, gv, rho, gd, ob.op, ob.n, blockIdx.x * BX,
                               blockIdx.y * BY * FORCE_ROWS);
 }
 
+template <typename Op, int CAP>
+OpBlock<Op, CAP> op_block(const Op* ops, int n) {
+    OpBlock<Op, CAP> ob;
+    ob.n = n;
+    for (int i = 0; i < n; ++i) ob.op[i] = ops[i];
+    return ob;
+}
+
 __global__ void __launch_bounds__(BX* BY) k_advect(const float2* __restrict__ vin, float2* __restrict__ vout,
-             const uint8_t* __restrict__ mask, Grid g, const StepParams* __restrict__ sp) {
+             const uint8_t* __restrict__ mask, Grid g, const __grid_constant__ StepParams spv) {
+    pdl_enter();
+    const StepParams* sp = &spv;
     NX_CELLS(cell_advect(vin, vout, mask, g, sp, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_calc_vorticity(const float2* __restrict__ v, float* __restrict__ w, Grid g) {
+    pdl_enter();
     NX_CELLS(cell_calc_vorticity(v, w, g, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_apply_vorticity(const float2* __restrict__ vin, float2* __restrict__ vout,
-                      const float* __restrict__ w, Grid g, const StepParams* __restrict__ sp) {
+                      const float* __restrict__ w, Grid g, const __grid_constant__ StepParams spv) {
+    pdl_enter();
+    const StepParams* sp = &spv;
     NX_CELLS(cell_apply_vorticity(vin, vout, w, g, sp, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_viscosity(const float2* __restrict__ vin, float2* __restrict__ vout, Grid g,
-                const StepParams* __restrict__ sp) {
+                const __grid_constant__ StepParams spv) {
+    pdl_enter();
+    const StepParams* sp = &spv;
     NX_CELLS(cell_viscosity(vin, vout, g, sp, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_divergence(const float2* __restrict__ v, const uint8_t* __restrict__ mask,
                  float* __restrict__ div, uint8_t* __restrict__ flags, float* __restrict__ p1,
-                 Grid g, const StepParams* __restrict__ sp) {
+                 Grid g, const __grid_constant__ StepParams spv) {
+    pdl_enter();
+    const StepParams* sp = &spv;
     NX_CELLS(cell_divergence(v, mask, div, flags, p1, g, sp, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_subtract_gradient(const float2* __restrict__ vin, float2* __restrict__ vout,
                         const float* __restrict__ p, const uint8_t* __restrict__ flags,
                         Grid g) {
+    pdl_enter();
     NX_CELLS(cell_subtract_gradient(vin, vout, p, flags, g, x, y));
 }
 
 __global__ void __launch_bounds__(BX* BY) k_density_advect(const float* __restrict__ rin, float* __restrict__ rout, Grid gd,
                      const float2* __restrict__ v, const uint8_t* __restrict__ mask, Grid gv,
-                     const StepParams* __restrict__ sp) {
+                     const __grid_constant__ StepParams spv) {
+    pdl_enter();
+    const StepParams* sp = &spv;
     NX_CELLS(cell_density_advect(rin, rout, gd, v, mask, gv, sp, x, y));
 }
 
@@ -99,7 +125,9 @@ constexpr int VW_W = VT_W + 2, VW_H = VT_H + 2;  // staged curl
 
 __global__ void __launch_bounds__(BX* BY)
     k_vorticity(const float2* __restrict__ vin, float2* __restrict__ vout, float* __restrict__ w,
-                Grid g, const StepParams* __restrict__ sp) {
+                Grid g, const __grid_constant__ StepParams spv) {
+    pdl_enter();
+    const StepParams* sp = &spv;
     __shared__ float2 sv[VV_H][VV_W];
     __shared__ float sw[VW_H][VW_W];
     const int x0 = blockIdx.x * VT_W, y0 = blockIdx.y * VT_H;
@@ -185,7 +213,9 @@ __device__ __forceinline__ VRow load_vrow(const float2* __restrict__ v,
 __global__ void __launch_bounds__(32 * ST_WARPS)
     k_divergence_st(const float2* __restrict__ v, const uint8_t* __restrict__ mask,
                     float* __restrict__ div, uint8_t* __restrict__ flags, float* __restrict__ p1,
-                    Grid g, const StepParams* __restrict__ sp) {
+                    Grid g, const __grid_constant__ StepParams spv) {
+    pdl_enter();
+    const StepParams* sp = &spv;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int c = blockIdx.x * ST_COLS + warp * 64 + 2 * lane;  // this lane's first column
     const int y0 = blockIdx.y * ST_ROWS;
@@ -245,6 +275,7 @@ __global__ void __launch_bounds__(32 * ST_WARPS)
 __global__ void __launch_bounds__(32 * ST_WARPS)
     k_subtract_gradient_st(const float2* __restrict__ vin, float2* __restrict__ vout,
                            const float* __restrict__ p, const uint8_t* __restrict__ flags, Grid g) {
+    pdl_enter();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int c = blockIdx.x * ST_COLS + warp * 64 + 2 * lane;
     const int y0 = blockIdx.y * ST_ROWS;
@@ -310,7 +341,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 __global__ void __launch_bounds__(RES_THREADS)
     k_residual(const float* __restrict__ p, const float* __restrict__ div,
                const uint8_t* __restrict__ mask, const uint8_t* __restrict__ flags, Grid g,
-               const StepParams* __restrict__ sp, double* __restrict__ partials) {
+               const __grid_constant__ StepParams spv, double* __restrict__ partials) {
+    const StepParams* sp = &spv;
     double acc[5] = {0, 0, 0, 0, 0};
     const long total = (long)g.W * g.H;
     const long base = (long)blockIdx.x * RES_THREADS * RES_CELLS_PER_THREAD + threadIdx.x;
@@ -427,78 +459,102 @@ cudaError_t launch_residual_labels(const float* p, const float* div, const uint8
     return cudaGetLastError();
 }
 
+bool pdl_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("NATRIX_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 cudaError_t launch_obstacles(uint8_t* mask, Grid g, const ShapeOp* ops, int n, int fresh,
                              cudaStream_t st) {
-    k_obstacles<<<dim3((g.W + BX - 1) / BX, (g.H + BY * FORCE_ROWS - 1) / (BY * FORCE_ROWS)),
-                  dim3(BX, BY), 0, st>>>(mask, g, ops, n, fresh);
-    return cudaGetLastError();
+    if (n < 0 || n > kMaxOpsPerLaunch) return cudaErrorInvalidValue;
+    const dim3 grid((g.W + BX - 1) / BX, (g.H + BY * FORCE_ROWS - 1) / (BY * FORCE_ROWS));
+    const bool pdl = pdl_enabled();
+    if (n <= 16)
+        return launch_kernel(pdl, k_obstacles<16>, grid, dim3(BX, BY), 0, st, mask, g,
+                             op_block<ShapeOp, 16>(ops, n), fresh);
+    if (n <= 64)
+        return launch_kernel(pdl, k_obstacles<64>, grid, dim3(BX, BY), 0, st, mask, g,
+                             op_block<ShapeOp, 64>(ops, n), fresh);
+    return launch_kernel(pdl, k_obstacles<kMaxOpsPerLaunch>, grid, dim3(BX, BY), 0, st, mask, g,
+                         op_block<ShapeOp, kMaxOpsPerLaunch>(ops, n), fresh);
 }
 
 cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const ForceOp* ops,
                            int n, cudaStream_t st) {
+    if (n < 0 || n > kMaxOpsPerLaunch) return cudaErrorInvalidValue;
     Grid gg = vel ? gv : gd;
     if (vel && rho) gg = Grid{gv.W > gd.W ? gv.W : gd.W, gv.H > gd.H ? gv.H : gd.H, 0};
-    k_forcing<<<dim3((gg.W + BX - 1) / BX, (gg.H + BY * FORCE_ROWS - 1) / (BY * FORCE_ROWS)),
-                dim3(BX, BY), 0, st>>>(vel, gv, rho, gd, ops, n);
-    return cudaGetLastError();
+    const dim3 grid((gg.W + BX - 1) / BX, (gg.H + BY * FORCE_ROWS - 1) / (BY * FORCE_ROWS));
+    const bool pdl = pdl_enabled();
+    if (n <= 16)
+        return launch_kernel(pdl, k_forcing<16>, grid, dim3(BX, BY), 0, st, vel, gv, rho, gd,
+                             op_block<ForceOp, 16>(ops, n));
+    if (n <= 64)
+        return launch_kernel(pdl, k_forcing<64>, grid, dim3(BX, BY), 0, st, vel, gv, rho, gd,
+                             op_block<ForceOp, 64>(ops, n));
+    return launch_kernel(pdl, k_forcing<kMaxOpsPerLaunch>, grid, dim3(BX, BY), 0, st, vel, gv,
+                         rho, gd, op_block<ForceOp, kMaxOpsPerLaunch>(ops, n));
 }
 
 cudaError_t launch_advect(const float2* vin, float2* vout, const uint8_t* mask, Grid g,
-                          const StepParams* sp, cudaStream_t st) {
-    k_advect<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(vin, vout, mask, g, sp);
-    return cudaGetLastError();
+                          const StepParams& sp, cudaStream_t st) {
+    return launch_kernel(pdl_enabled(), k_advect, grid_cpt(g), dim3(BX, BY), 0, st, vin, vout,
+                         mask, g, sp);
 }
 
 cudaError_t launch_calc_vorticity(const float2* v, float* w, Grid g, cudaStream_t st) {
-    k_calc_vorticity<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(v, w, g);
-    return cudaGetLastError();
+    return launch_kernel(pdl_enabled(), k_calc_vorticity, grid_cpt(g), dim3(BX, BY), 0, st, v, w,
+                         g);
 }
 
 cudaError_t launch_apply_vorticity(const float2* vin, float2* vout, const float* w, Grid g,
-                                   const StepParams* sp, cudaStream_t st) {
-    k_apply_vorticity<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(vin, vout, w, g, sp);
-    return cudaGetLastError();
+                                   const StepParams& sp, cudaStream_t st) {
+    return launch_kernel(pdl_enabled(), k_apply_vorticity, grid_cpt(g), dim3(BX, BY), 0, st, vin,
+                         vout, w, g, sp);
 }
 
 cudaError_t launch_vorticity(const float2* vin, float2* vout, float* w, Grid g,
-                             const StepParams* sp, cudaStream_t st) {
-    k_vorticity<<<dim3((g.W + VT_W - 1) / VT_W, (g.H + VT_H - 1) / VT_H), dim3(BX, BY), 0, st>>>(
-        vin, vout, w, g, sp);
-    return cudaGetLastError();
+                             const StepParams& sp, cudaStream_t st) {
+    return launch_kernel(pdl_enabled(), k_vorticity,
+                         dim3((g.W + VT_W - 1) / VT_W, (g.H + VT_H - 1) / VT_H), dim3(BX, BY), 0,
+                         st, vin, vout, w, g, sp);
 }
 
-cudaError_t launch_viscosity(const float2* vin, float2* vout, Grid g, const StepParams* sp,
+cudaError_t launch_viscosity(const float2* vin, float2* vout, Grid g, const StepParams& sp,
                              cudaStream_t st) {
-    k_viscosity<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(vin, vout, g, sp);
-    return cudaGetLastError();
+    return launch_kernel(pdl_enabled(), k_viscosity, grid_cpt(g), dim3(BX, BY), 0, st, vin, vout,
+                         g, sp);
 }
 
 cudaError_t launch_divergence(const float2* v, const uint8_t* mask, float* div,
-                              uint8_t* flags, float* p1, Grid g, const StepParams* sp,
+                              uint8_t* flags, float* p1, Grid g, const StepParams& sp,
                               cudaStream_t st) {
     if (g.W % 2 == 0 && g.W >= 2)
-        k_divergence_st<<<dim3((g.W + ST_COLS - 1) / ST_COLS, (g.H + ST_ROWS - 1) / ST_ROWS),
-                          32 * ST_WARPS, 0, st>>>(v, mask, div, flags, p1, g, sp);
-    else
-        k_divergence<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(v, mask, div, flags, p1, g, sp);
-    return cudaGetLastError();
+        return launch_kernel(pdl_enabled(), k_divergence_st,
+                             dim3((g.W + ST_COLS - 1) / ST_COLS, (g.H + ST_ROWS - 1) / ST_ROWS),
+                             dim3(32 * ST_WARPS), 0, st, v, mask, div, flags, p1, g, sp);
+    return launch_kernel(pdl_enabled(), k_divergence, grid_cpt(g), dim3(BX, BY), 0, st, v, mask,
+                         div, flags, p1, g, sp);
 }
 
 cudaError_t launch_subtract_gradient(const float2* vin, float2* vout, const float* p,
                                      const uint8_t* flags, Grid g, cudaStream_t st) {
     if (g.W % 2 == 0 && g.W >= 2)
-        k_subtract_gradient_st<<<dim3((g.W + ST_COLS - 1) / ST_COLS, (g.H + ST_ROWS - 1) / ST_ROWS),
-                                 32 * ST_WARPS, 0, st>>>(vin, vout, p, flags, g);
-    else
-        k_subtract_gradient<<<grid_cpt(g), dim3(BX, BY), 0, st>>>(vin, vout, p, flags, g);
-    return cudaGetLastError();
+        return launch_kernel(pdl_enabled(), k_subtract_gradient_st,
+                             dim3((g.W + ST_COLS - 1) / ST_COLS, (g.H + ST_ROWS - 1) / ST_ROWS),
+                             dim3(32 * ST_WARPS), 0, st, vin, vout, p, flags, g);
+    return launch_kernel(pdl_enabled(), k_subtract_gradient, grid_cpt(g), dim3(BX, BY), 0, st, vin,
+                         vout, p, flags, g);
 }
 
 cudaError_t launch_density_advect(const float* rin, float* rout, Grid gd, const float2* v,
-                                  const uint8_t* mask, Grid gv, const StepParams* sp,
+                                  const uint8_t* mask, Grid gv, const StepParams& sp,
                                   cudaStream_t st) {
-    k_density_advect<<<grid_cpt(gd), dim3(BX, BY), 0, st>>>(rin, rout, gd, v, mask, gv, sp);
-    return cudaGetLastError();
+    return launch_kernel(pdl_enabled(), k_density_advect, grid_cpt(gd), dim3(BX, BY), 0, st, rin,
+                         rout, gd, v, mask, gv, sp);
 }
 
 int residual_partials(Grid g) {
@@ -508,7 +564,7 @@ int residual_partials(Grid g) {
 }
 
 cudaError_t launch_residual(const float* p, const float* div, const uint8_t* mask,
-                            const uint8_t* flags, Grid g, const StepParams* sp,
+                            const uint8_t* flags, Grid g, const StepParams& sp,
                             double* partials, double* out, cudaStream_t st) {
     const int nb = residual_partials(g);
     k_residual<<<nb, RES_THREADS, 0, st>>>(p, div, mask, flags, g, sp, partials);
