@@ -98,6 +98,9 @@ struct natrix_sim {
     int res_blocks = 0;
     JacobiMaps maps{};             // host copy (encoded at creation)
     JacobiMaps* d_maps = nullptr;  // device copy the sweep kernels read
+    TileMarks marks{};             // sweep tiles next to obstacles (geometry; words = 0: off)
+    uint32_t* d_marks[2] = {};     // this step's marks / the previous step's
+    int marks_cur = 0;
     std::vector<ForceOp> fq;
     std::vector<ShapeOp> sq;
     bool mask_reset_pending = true;  // the mask memory does not hold the current obstacles
@@ -145,6 +148,8 @@ void free_sim(natrix_sim* s) {
     cudaFree(s->d_status);
     cudaFree(s->d_res);
     cudaFree(s->d_maps);
+    cudaFree(s->d_marks[0]);
+    cudaFree(s->d_marks[1]);
     if (s->h_res) cudaFreeHost(s->h_res);
     delete s;
 }
@@ -223,7 +228,7 @@ int run_jacobi(natrix_sim* s, int sweeps, cudaStream_t st) {
     while (sweeps > 0) {
         const int k = sweeps < per ? sweeps : per;
         NX_LAUNCH(s, launch_jacobi(s->d_maps, s->maps.config, s->p, s->p_cur, s->g, k,
-                                   s->d_status, st));
+                                   s->d_marks[s->marks_cur], s->d_status, st));
         s->p_cur ^= 1;
         sweeps -= k;
         ++launches;
@@ -346,9 +351,15 @@ int natrix_create(int32_t width, int32_t height, natrix_sim** out) {
     e = cudaMalloc(&s->d_maps, sizeof(JacobiMaps));
     if (e == cudaSuccess)
         e = cudaMemcpy(s->d_maps, &s->maps, sizeof(JacobiMaps), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && jacobi_tile_marks(s->maps.config, s->g, &s->marks)) {
+        for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+            e = cudaMalloc(&s->d_marks[i], (size_t)s->marks.words * 4);
+            if (e == cudaSuccess) e = cudaMemset(s->d_marks[i], 0, (size_t)s->marks.words * 4);
+        }
+    }
     if (e != cudaSuccess) {
         free_sim(s);
-        return fail(NATRIX_ECUDA, "uploading tensor maps: %s", cudaGetErrorString(e));
+        return fail(NATRIX_ECUDA, "setting up the sweep tiles: %s", cudaGetErrorString(e));
     }
     *out = s;
     return NATRIX_OK;
@@ -443,7 +454,14 @@ int natrix_step(natrix_sim* s, float dt, void* stream) {
         NX_LAUNCH(s, launch_viscosity(s->vel[cur], s->vel[3 - cur], g, sp, st));
         cur = 3 - cur;
     }
-    NX_LAUNCH(s, launch_divergence(s->vel[cur], s->mask, s->div, s->flags, s->p[0], g, sp, st));
+    TileMarks tm{};
+    if (s->marks.words > 0) {
+        s->marks_cur ^= 1;
+        tm = s->marks;
+        tm.mark = s->d_marks[s->marks_cur];
+        tm.clear = s->d_marks[1 - s->marks_cur];
+    }
+    NX_LAUNCH(s, launch_divergence(s->vel[cur], s->mask, s->div, s->flags, s->p[0], g, sp, tm, st));
     s->p_cur = 0;
     rc = run_jacobi(s, s->prm.iterations - 1, st);
     if (rc) return rc;

@@ -395,7 +395,13 @@ __device__ __forceinline__ void cell_density_advect(const float* __restrict__ ri
         }
     }
     const Corners cv = corners(nx, ny, gv.W, gv.H);
-    float2 u = sample_vel(v, gv.P, cv);
+    // On a cell centre (equal grid sizes) the four corners are one cell and
+    // the bilinear mix of a finite velocity returns it (a -0 comes back as
+    // +0, which the backtrace x - u*dt*speed cannot tell apart), so one load
+    // gives the same result.
+    float2 u = (cv.lo_x == cv.hi_x && cv.lo_y == cv.hi_y && cv.dx == 0.0f && cv.dy == 0.0f)
+                   ? __ldg(v + (size_t)cv.lo_y * gv.P + cv.lo_x)
+                   : sample_vel(v, gv.P, cv);
     u.x = u.x * ((float)gd.W / (float)gv.W);
     u.y = u.y * ((float)gd.H / (float)gv.H);
     const float dt = sp->dt, speed = sp->d_speed;

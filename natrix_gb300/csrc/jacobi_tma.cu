@@ -106,10 +106,62 @@ struct GridJobs {
     float* pout;
     Grid g;
     int sweeps, tiles_x, n, tx, ty;
+    const uint32_t* slow;  // tiles next to obstacles (TileMarks bits), or null
     __device__ __forceinline__ TileJob operator()(int t) const {
         return TileJob{p, d, f, pout, g, sweeps, (t % tiles_x) * tx, (t / tiles_x) * ty};
     }
 };
+
+// Most tiles one CTA of a balanced launch takes (kMaxBalancedTiles over the
+// SM count, rounded up, with room to spare).
+constexpr int kMaxCtaTiles = 16;
+
+template <class Jobs>
+__device__ __forceinline__ const uint32_t* slow_marks(const Jobs&) { return nullptr; }
+__device__ __forceinline__ const uint32_t* slow_marks(const GridJobs& j) { return j.slow; }
+
+// Balanced deal of n tiles to G CTAs, computed by one warp for CTA b.  Order:
+// the marked (slow) tiles, then the others, each in index order; position p
+// of that order goes to CTA p mod G in even rounds and G - 1 - (p mod G) in
+// odd rounds, so CTA b takes the positions b, 2G - 1 - b, 2G + b, ... and a
+// slow tile dealt early is followed by a plain tile dealt late.  Writes the
+// tiles to out[] and returns their count (a permutation of 0..n-1 over all
+// CTAs).  Needs n <= 32 * 32.
+__device__ int balanced_tiles(const uint32_t* slow, int n, int b, int G, int* out) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int base = lane * 32;
+    const uint32_t valid = base >= n ? 0u : (n - base >= 32 ? FULL : (1u << (n - base)) - 1u);
+    const uint32_t ws = (base < n ? slow[lane] : 0u) & valid;
+    const uint32_t wz = ~ws & valid;
+    int is = __popc(ws), iz = __popc(wz);  // inclusive prefix counts over lanes
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int a = __shfl_up_sync(FULL, is, o), c = __shfl_up_sync(FULL, iz, o);
+        if (lane >= o) {
+            is += a;
+            iz += c;
+        }
+    }
+    const int n_slow = __shfl_sync(FULL, is, 31);
+    int count = 0;
+    for (int k = 0;; ++k) {
+        const int p = (k & 1) ? (k + 1) * G - 1 - b : k * G + b;
+        if (p >= n || count >= kMaxCtaTiles) break;
+        const bool s = p < n_slow;
+        const int q = s ? p : p - n_slow;
+        const int incl = s ? is : iz;
+        uint32_t w = s ? ws : wz;
+        const unsigned hit = __ballot_sync(FULL, incl > q);
+        const int src = __ffs(hit) - 1;  // lane holding the q-th tile of its kind
+        if (lane == src) {
+            for (int r = q - (incl - __popc(w)); r > 0; --r) w &= w - 1u;
+            out[count] = base + __ffs(w) - 1;
+        }
+        ++count;
+    }
+    return count;
+}
 
 // Jobs of a batch: item t names a simulation, a tile origin, a sweep count
 // and the source pressure buffer.
@@ -288,16 +340,36 @@ __global__ void __launch_bounds__(C::THREADS, 1)
     const int c0 = lane * 4, r0 = w * R;
 
     pdl_enter();
-    int t = blockIdx.x;
-    if (t >= jobs.n) return;
+    // this CTA's tiles: the balanced deal when the tiles are marked, else
+    // blockIdx.x + k * gridDim.x
+    __shared__ int s_tiles[kMaxCtaTiles];
+    __shared__ int s_count;
+    const uint32_t* slow = slow_marks(jobs);
+    const bool balanced = slow != nullptr && jobs.n <= kMaxBalancedTiles &&
+                          (jobs.n + (int)gridDim.x - 1) / (int)gridDim.x <= kMaxCtaTiles;
+    if (balanced) {
+        if (w == 0) {
+            const int cnt = balanced_tiles(slow, jobs.n, blockIdx.x, gridDim.x, s_tiles);
+            if (lane == 0) s_count = cnt;
+        }
+        __syncthreads();
+    }
+    const int n_mine = balanced ? s_count
+                                : (jobs.n > (int)blockIdx.x
+                                       ? (jobs.n - 1 - (int)blockIdx.x) / (int)gridDim.x + 1
+                                       : 0);
+    auto tile_of = [&](int k) {
+        return balanced ? s_tiles[k] : (int)blockIdx.x + k * (int)gridDim.x;
+    };
+    if (n_mine == 0) return;
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
         fence_barrier_init();
-        issue_tile_loads<C>(smem, bar, jobs(t));
+        issue_tile_loads<C>(smem, bar, jobs(tile_of(0)));
     }
     uint32_t parity = 0;
-    for (; t < jobs.n; t += gridDim.x, parity ^= 1u) {
-        const TileJob job = jobs(t);
+    for (int k = 0; k < n_mine; ++k, parity ^= 1u) {
+        const TileJob job = jobs(tile_of(k));
         if (threadIdx.x == 0) {
             bool ok = wait_phase(bar, parity);
             if (!ok) {
@@ -333,9 +405,9 @@ __global__ void __launch_bounds__(C::THREADS, 1)
             if (__any_sync(FULL, (f[r] & ~side) != 0u)) slow |= 1u << r;
         }
         __syncthreads();  // staging consumed: prefetch the next job into it
-        if (threadIdx.x == 0 && t + (int)gridDim.x < jobs.n) {
+        if (threadIdx.x == 0 && k + 1 < n_mine) {
             fence_proxy_async();
-            issue_tile_loads<C>(smem, bar, jobs(t + gridDim.x));
+            issue_tile_loads<C>(smem, bar, jobs(tile_of(k + 1)));
         }
 
         for (int s = 0; s < job.sweeps; ++s) {
@@ -524,6 +596,33 @@ int jacobi_config(Grid g) {
     return rt_cost<RtB>(g) < rt_cost<RtA>(g) ? JACOBI_RT_B : JACOBI_RT_A;
 }
 
+template <class C>
+void rt_marks(Grid g, TileMarks* m) {
+    m->tx = C::TX;
+    m->ty = C::TY;
+    m->rx = C::RX;
+    m->ry = C::RY;
+    m->hxp = C::HXP;
+    m->halo = C::HALO;
+    m->tiles_x = (g.W + C::TX - 1) / C::TX;
+    m->tiles_y = (g.H + C::TY - 1) / C::TY;
+}
+
+bool jacobi_tile_marks(int config, Grid g, TileMarks* out) {
+    TileMarks m{};
+    if (config == JACOBI_RT_A)
+        rt_marks<RtA>(g, &m);
+    else if (config == JACOBI_RT_B)
+        rt_marks<RtB>(g, &m);
+    else
+        return false;
+    const long tiles = (long)m.tiles_x * m.tiles_y;
+    if (tiles > kMaxBalancedTiles) return false;
+    m.words = (int)((tiles + 31) / 32);
+    *out = m;
+    return true;
+}
+
 void jacobi_tile(int config, int* tx, int* ty) {
     switch (config) {
         case JACOBI_RT_A: *tx = RtA::TX; *ty = RtA::TY; break;
@@ -549,13 +648,13 @@ bool jacobi_encode_maps_for(JacobiMaps* maps, int config, float* p0, float* p1, 
 }
 
 cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbuf[2], int src,
-                          Grid g, int sweeps, int* status, cudaStream_t st) {
+                          Grid g, int sweeps, const uint32_t* slow, int* status, cudaStream_t st) {
     if (sweeps < 1 || sweeps > jacobi_max_sweeps_per_launch()) return cudaErrorInvalidValue;
     int tx, ty;
     jacobi_tile(config, &tx, &ty);
     const int tiles_x = (g.W + tx - 1) / tx, tiles_y = (g.H + ty - 1) / ty;
     const GridJobs jobs{&d_maps->p[src], &d_maps->div, &d_maps->flags, pbuf[1 - src], g,
-                        sweeps, tiles_x, tiles_x * tiles_y, tx, ty};
+                        sweeps, tiles_x, tiles_x * tiles_y, tx, ty, slow};
     const bool pdl = pdl_enabled();
     if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st, pdl);
     if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st, pdl);

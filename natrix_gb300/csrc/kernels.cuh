@@ -60,6 +60,19 @@ struct OpBlock {
     Op op[CAP];
 };
 
+// Tiles of the persistent register-tiled sweep whose region holds a cell next
+// to an obstacle (one bit per tile, row-major).  Such tiles take the per-cell
+// select path and cost up to ~1.7x a plain tile; the divergence kernel marks
+// them and the sweep launch deals them to CTAs paired with plain tiles.  The
+// marks only steer scheduling: every order computes the same values.
+constexpr int kMaxBalancedTiles = 1024;  // one 32-bit word per lane of one warp
+struct TileMarks {
+    uint32_t* mark;   // bits of this step, zero on entry (null: no marking)
+    uint32_t* clear;  // bits of the previous step, zeroed for the next one
+    int words;
+    int tx, ty, rx, ry, hxp, halo, tiles_x, tiles_y;
+};
+
 // Record `msg` as the calling thread's natrix_last_error() and return `code`.
 int set_last_error(int code, const char* msg);
 
@@ -107,9 +120,10 @@ cudaError_t launch_apply_vorticity(const float2* vin, float2* vout, const float*
                                    const StepParams& sp, cudaStream_t st);
 cudaError_t launch_viscosity(const float2* vin, float2* vout, Grid g, const StepParams& sp,
                              cudaStream_t st);
+// `marks` (may have a null `mark`) receives the tiles with obstacle rows.
 cudaError_t launch_divergence(const float2* v, const uint8_t* mask, float* div,
                               uint8_t* flags, float* p1, Grid g, const StepParams& sp,
-                              cudaStream_t st);
+                              const TileMarks& marks, cudaStream_t st);
 cudaError_t launch_subtract_gradient(const float2* vin, float2* vout, const float* p,
                                      const uint8_t* flags, Grid g, cudaStream_t st);
 cudaError_t launch_density_advect(const float* rin, float* rout, Grid gd, const float2* v,
@@ -166,13 +180,18 @@ int jacobi_max_sweeps_per_launch();
 int jacobi_config(Grid g);
 // Output tile of a configuration.
 void jacobi_tile(int config, int* tx, int* ty);
+
+// Tile geometry of a register-tiled configuration for grid g (false for the
+// shared-memory configuration or more than kMaxBalancedTiles tiles).
+bool jacobi_tile_marks(int config, Grid g, TileMarks* out);
 // Encode the tensor maps of the buffers for a configuration (false + message on error).
 bool jacobi_encode_maps_for(JacobiMaps* maps, int config, float* p0, float* p1, float* div,
                             uint8_t* flags, Grid g, const char** err);
 // `sweeps` (1..max) Jacobi sweeps of one grid from pbuf[src] into pbuf[1 - src];
 // `d_maps` is the device copy of the grid's maps.
+// `slow` (device, may be null) holds the tile marks of the current step.
 cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbuf[2], int src,
-                          Grid g, int sweeps, int* status, cudaStream_t st);
+                          Grid g, int sweeps, const uint32_t* slow, int* status, cudaStream_t st);
 // One batched launch: every item is one tile of one simulation (device arrays).
 cudaError_t launch_jacobi_batch(int config, const JacobiBatchItem* items, int n_items,
                                 const JacobiBatchSim* sims, int* status, cudaStream_t st);

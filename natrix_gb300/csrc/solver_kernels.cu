@@ -5,6 +5,7 @@
 // One thread per cell, 32x8 blocks (a warp spans 32 consecutive cells of a
 // row, so float2 velocity loads and stores coalesce into 256-byte segments).
 // Compiled with -fmad=false: see common.cuh for the arithmetic contract.
+#include <climits>
 #include <cstdlib>
 
 #include "cells.cuh"
@@ -88,11 +89,38 @@ __global__ void __launch_bounds__(BX* BY) k_viscosity(const float2* __restrict__
     NX_CELLS(cell_viscosity(vin, vout, g, sp, x, y));
 }
 
+// Zero the previous step's tile marks (first block of the grid).
+__device__ __forceinline__ void clear_marks(const TileMarks& tm) {
+    if (tm.clear && blockIdx.x == 0 && blockIdx.y == 0)
+        for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < tm.words;
+             i += blockDim.x * blockDim.y)
+            tm.clear[i] = 0u;
+}
+
+__device__ __forceinline__ int ceil_div_signed(int a, int b) {
+    return a > 0 ? (a + b - 1) / b : -((-a) / b);
+}
+
+// Mark every sweep tile whose region meets the cell box [x0, x1] x [y0, y1]
+// (coordinates >= 0).
+__device__ void mark_tiles(const TileMarks& tm, int x0, int x1, int y0, int y1) {
+    const int i0 = max(ceil_div_signed(x0 + tm.hxp - tm.rx + 1, tm.tx), 0);
+    const int i1 = min((x1 + tm.hxp) / tm.tx, tm.tiles_x - 1);
+    const int j0 = max(ceil_div_signed(y0 + tm.halo - tm.ry + 1, tm.ty), 0);
+    const int j1 = min((y1 + tm.halo) / tm.ty, tm.tiles_y - 1);
+    for (int j = j0; j <= j1; ++j)
+        for (int i = i0; i <= i1; ++i) {
+            const int t = j * tm.tiles_x + i;
+            atomicOr(tm.mark + (t >> 5), 1u << (t & 31));
+        }
+}
+
 __global__ void __launch_bounds__(BX* BY) k_divergence(const float2* __restrict__ v, const uint8_t* __restrict__ mask,
                  float* __restrict__ div, uint8_t* __restrict__ flags, float* __restrict__ p1,
-                 Grid g, const __grid_constant__ StepParams spv) {
+                 Grid g, const __grid_constant__ StepParams spv, const __grid_constant__ TileMarks tm) {
     pdl_enter();
     const StepParams* sp = &spv;
+    clear_marks(tm);  // this variant leaves the marks empty (static tile order)
     NX_CELLS(cell_divergence(v, mask, div, flags, p1, g, sp, x, y));
 }
 
@@ -213,9 +241,11 @@ __device__ __forceinline__ VRow load_vrow(const float2* __restrict__ v,
 __global__ void __launch_bounds__(32 * ST_WARPS)
     k_divergence_st(const float2* __restrict__ v, const uint8_t* __restrict__ mask,
                     float* __restrict__ div, uint8_t* __restrict__ flags, float* __restrict__ p1,
-                    Grid g, const __grid_constant__ StepParams spv) {
+                    Grid g, const __grid_constant__ StepParams spv,
+                    const __grid_constant__ TileMarks tm) {
     pdl_enter();
     const StepParams* sp = &spv;
+    clear_marks(tm);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int c = blockIdx.x * ST_COLS + warp * 64 + 2 * lane;  // this lane's first column
     const int y0 = blockIdx.y * ST_ROWS;
@@ -226,6 +256,7 @@ __global__ void __launch_bounds__(32 * ST_WARPS)
     VRow up = load_vrow(v, mask, g, y0 - 1, cc, mz);
     VRow mid = load_vrow(v, mask, g, y0, cc, mz);
     const int y1 = min(y0 + ST_ROWS, g.H);
+    int near_lo = INT_MAX, near_hi = -1;  // rows of this lane with a cell next to an obstacle
     for (int y = y0; y < y1; ++y) {
         const VRow dn = load_vrow(v, mask, g, y + 1, cc, mz);
         // left neighbour of column c (clamped), right neighbour of c + 1
@@ -263,12 +294,25 @@ __global__ void __launch_bounds__(32 * ST_WARPS)
             if (y == 0 || ob1) f1 |= NB_B;
             if (y == g.H - 1 || ot1) f1 |= NB_T;
             *reinterpret_cast<uint16_t*>(flags + row + c) = (uint16_t)(f0 | (f1 << 8));
+            if (ol0 | or0 | ob0 | ot0 | ol1 | or1 | ob1 | ot1) {
+                near_lo = min(near_lo, y);
+                near_hi = y;
+            }
             if (p1)
                 *reinterpret_cast<float2*>(p1 + row + c) =
                     make_float2((0.0f - b0) * 0.25f, (0.0f - b1) * 0.25f);
         }
         up = mid;
         mid = dn;
+    }
+    if (tm.mark) {
+        // bounding box of this warp's cells next to an obstacle
+        const bool near = near_hi >= 0;
+        const int ylo = __reduce_min_sync(FULL, near ? near_lo : INT_MAX);
+        const int yhi = __reduce_max_sync(FULL, near ? near_hi : -1);
+        const int xlo = __reduce_min_sync(FULL, near ? c : INT_MAX);
+        const int xhi = __reduce_max_sync(FULL, near ? c + 1 : -1);
+        if (lane == 0 && yhi >= 0) mark_tiles(tm, xlo, xhi, ylo, yhi);
     }
 }
 
@@ -531,13 +575,14 @@ cudaError_t launch_viscosity(const float2* vin, float2* vout, Grid g, const Step
 
 cudaError_t launch_divergence(const float2* v, const uint8_t* mask, float* div,
                               uint8_t* flags, float* p1, Grid g, const StepParams& sp,
-                              cudaStream_t st) {
+                              const TileMarks& marks, cudaStream_t st) {
+    if (marks.words > kMaxBalancedTiles / 32) return cudaErrorInvalidValue;
     if (g.W % 2 == 0 && g.W >= 2)
         return launch_kernel(pdl_enabled(), k_divergence_st,
                              dim3((g.W + ST_COLS - 1) / ST_COLS, (g.H + ST_ROWS - 1) / ST_ROWS),
-                             dim3(32 * ST_WARPS), 0, st, v, mask, div, flags, p1, g, sp);
+                             dim3(32 * ST_WARPS), 0, st, v, mask, div, flags, p1, g, sp, marks);
     return launch_kernel(pdl_enabled(), k_divergence, grid_cpt(g), dim3(BX, BY), 0, st, v, mask,
-                         div, flags, p1, g, sp);
+                         div, flags, p1, g, sp, marks);
 }
 
 cudaError_t launch_subtract_gradient(const float2* vin, float2* vout, const float* p,
