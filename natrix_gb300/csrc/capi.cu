@@ -193,22 +193,31 @@ int flush_shapes(natrix_sim* s, cudaStream_t st) {
     return NATRIX_OK;
 }
 
+// zeroed (may be null): ask the last launch to write the velocity border as
+// zero (the start of a step, shader.InitBoundaries.comp); set to whether it
+// did, which needs a velocity op in that launch.
 int flush_force_list(natrix_sim* s, std::vector<ForceOp>& q, float2* vel, Grid gv, float* rho,
-                     Grid gd, cudaStream_t st) {
+                     Grid gd, cudaStream_t st, bool* zeroed = nullptr) {
+    if (zeroed) *zeroed = false;
     size_t done = 0;
     while (done < q.size()) {
         const int n = (int)std::min<size_t>(kMaxOpsPerLaunch, q.size() - done);
-        NX_LAUNCH(s, launch_forcing(vel, gv, rho, gd, q.data() + done, n, st));
+        bool zero = false;
+        if (zeroed && vel && done + n == q.size())
+            for (int k = 0; k < n && !zero; ++k)
+                zero = q[done + k].kind == FORCE_CONE_VELOCITY || q[done + k].kind == FORCE_GAUSS;
+        NX_LAUNCH(s, launch_forcing(vel, gv, rho, gd, q.data() + done, n, zero ? 1 : 0, st));
+        if (zero) *zeroed = true;
         done += n;
     }
     q.clear();
     return NATRIX_OK;
 }
 
-int flush_fluid(natrix_sim* s, cudaStream_t st) {
+int flush_fluid(natrix_sim* s, cudaStream_t st, bool* border_zeroed = nullptr) {
     int rc = flush_shapes(s, st);
     if (rc) return rc;
-    return flush_force_list(s, s->fq, s->vel[0], s->g, nullptr, Grid{}, st);
+    return flush_force_list(s, s->fq, s->vel[0], s->g, nullptr, Grid{}, st, border_zeroed);
 }
 
 int flush_density(natrix_density* d, cudaStream_t st) {
@@ -438,13 +447,14 @@ int natrix_step(natrix_sim* s, float dt, void* stream) {
     if (!s->prm.simulate) return NATRIX_OK;
     DeviceGuard dg(s->device);
     cudaStream_t st = stream_of(s, stream);
-    int rc = flush_fluid(s, st);
+    bool border_zeroed = false;
+    int rc = flush_fluid(s, st, s->prm.has_borders ? &border_zeroed : nullptr);
     if (rc) return rc;
     const bool mask_zero = s->mask_reset_pending;
     const StepParams sp = fluid_params(s, dt, mask_zero);
 
     const Grid g = s->g;
-    NX_LAUNCH(s, launch_advect(s->vel[0], s->vel[1], s->mask, g, sp, st));
+    NX_LAUNCH(s, launch_advect(s->vel[0], s->vel[1], s->mask, g, sp, border_zeroed, st));
     int cur = 1;
     if (s->prm.vorticity > 0.0f) {
         NX_LAUNCH(s, launch_vorticity(s->vel[cur], s->vel[3 - cur], s->vort, g, sp, st));

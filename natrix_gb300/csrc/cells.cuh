@@ -117,11 +117,15 @@ __device__ __forceinline__ bool op_is_velocity(int kind) {
     return kind == FORCE_CONE_VELOCITY || kind == FORCE_GAUSS;
 }
 
+// zero_border: after the ops, write the border cells of the velocity grid as
+// zero (shader.InitBoundaries.comp, which the reference dispatches next when
+// the step starts); only meaningful when the list holds a velocity op, since
+// then every cell is written.
 template <int ROWS = 1>
 __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
                                               float* __restrict__ rho, Grid gd,
                                               const ForceOp* __restrict__ ops, int n, int bx0,
-                                              int by0) {
+                                              int by0, bool zero_border = false) {
     __shared__ ForceOp s_ops[kMaxOpsPerLaunch];
     __shared__ int s_kept[kMaxOpsPerLaunch];
     const int tid = threadIdx.y * BX + threadIdx.x;
@@ -146,12 +150,19 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
                                       bx1, by0, by1);
             return false;
         });
+        // all rows' loads first (several DRAM reads in flight per thread)
+        float2 va[ROWS];
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            const int y = by0 + threadIdx.y + r * BY;
+            if (first_vel >= 0 && x < gv.W && y < gv.H) va[r] = vel[(size_t)y * gv.P + x];
+        }
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) {
             const int y = by0 + threadIdx.y + r * BY;
             if (first_vel < 0 || x >= gv.W || y >= gv.H) continue;
             const size_t i = (size_t)y * gv.P + x;
-            float2 a = vel[i];
+            float2 a = va[r];
             // the first velocity op culled for this block: it clamps the cell
             bool started = !(nk > 0 && s_kept[0] == first_vel);
             if (started) {
@@ -188,6 +199,8 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
                     started = true;
                 }
             }
+            if (zero_border && (x == 0 || x == gv.W - 1 || y == 0 || y == gv.H - 1))
+                a = make_float2(0.0f, 0.0f);
             vel[i] = a;
         }
         __syncthreads();  // s_kept is reused below
@@ -203,12 +216,18 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
                                                        op.r, bx0, bx1, by0, by1);
             return false;
         });
+        float ra[ROWS];
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            const int y = by0 + threadIdx.y + r * BY;
+            if (nk != 0 && x < gd.W && y < gd.H) ra[r] = rho[(size_t)y * gd.P + x];
+        }
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) {
             const int y = by0 + threadIdx.y + r * BY;
             if (nk == 0 || x >= gd.W || y >= gd.H) continue;
             const size_t i = (size_t)y * gd.P + x;
-            float a = rho[i];
+            float a = ra[r];
             for (int kk = 0; kk < nk; ++kk) {
                 const ForceOp& op = s_ops[s_kept[kk]];
                 if (op.kind == FORCE_GAUSS) {

@@ -108,10 +108,13 @@ void sim_count_launches(natrix_sim* sim, int n);
 // `ops` is host memory (n <= kMaxOpsPerLaunch), copied into the launch.
 cudaError_t launch_obstacles(uint8_t* mask, Grid g, const ShapeOp* ops, int n, int fresh,
                              cudaStream_t st);
+// zero_border: also write the velocity grid's border cells as zero after the
+// ops (takes effect when the list holds a velocity op).
 cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const ForceOp* ops,
-                           int n, cudaStream_t st);
+                           int n, int zero_border, cudaStream_t st);
+// border_zeroed: vin's border cells already hold zero (no test on read).
 cudaError_t launch_advect(const float2* vin, float2* vout, const uint8_t* mask, Grid g,
-                          const StepParams& sp, cudaStream_t st);
+                          const StepParams& sp, bool border_zeroed, cudaStream_t st);
 cudaError_t launch_calc_vorticity(const float2* v, float* w, Grid g, cudaStream_t st);
 // calc + apply in one pass (same results); writes the curl to w
 cudaError_t launch_vorticity(const float2* vin, float2* vout, float* w, Grid g,

@@ -49,10 +49,10 @@ __global__ void __launch_bounds__(BX* BY)
 template <int CAP>
 __global__ void __launch_bounds__(BX* BY)
     k_forcing(float2* __restrict__ vel, Grid gv, float* __restrict__ rho, Grid gd,
-              const __grid_constant__ OpBlock<ForceOp, CAP> ob) {
+              const __grid_constant__ OpBlock<ForceOp, CAP> ob, int zero_border) {
     pdl_enter();
     block_forcing<FORCE_ROWS>(vel, gv, rho, gd, ob.op, ob.n, blockIdx.x * BX,
-                              blockIdx.y * BY * FORCE_ROWS);
+                              blockIdx.y * BY * FORCE_ROWS, zero_border != 0);
 }
 
 template <typename Op, int CAP>
@@ -63,11 +63,55 @@ OpBlock<Op, CAP> op_block(const Op* ops, int n) {
     return ob;
 }
 
-__global__ void __launch_bounds__(BX* BY) k_advect(const float2* __restrict__ vin, float2* __restrict__ vout,
-             const uint8_t* __restrict__ mask, Grid g, const __grid_constant__ StepParams spv) {
+// shader.AdvectVelocity.comp:19-51 (cell_advect's arithmetic, 32-bit cell
+// indices).  ZB: border cells read as zero (shader.InitBoundaries.comp fused
+// on read); false when has_borders is off or when this step's forcing launch
+// already wrote the zero border in place, as the reference's InitBoundaries
+// dispatch does before advecting.
+template <bool ZB>
+__global__ void __launch_bounds__(BX* BY)
+    k_advect(const float2* __restrict__ vin, float2* __restrict__ vout,
+             const uint8_t* __restrict__ mask, Grid g, const __grid_constant__ StepParams sp) {
     pdl_enter();
-    const StepParams* sp = &spv;
-    NX_CELLS(cell_advect(vin, vout, mask, g, sp, x, y));
+    const int x = blockIdx.x * BX + threadIdx.x;
+    if (x >= g.W) return;
+    const bool mz = sp.mask_zero != 0;
+    const float dt = sp.dt, speed = sp.speed, diss = sp.dissipation;
+    const bool xb = ZB && (x == 0 || x == g.W - 1);
+    const float2 zero = make_float2(0.0f, 0.0f);
+    const int y0 = blockIdx.y * (BY * CPT) + threadIdx.y;
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+        const int y = y0 + k * BY;
+        if (y >= g.H) break;
+        const int i = y * g.P + x;
+        if (!mz && mask[i]) {
+            vout[i] = zero;
+            continue;
+        }
+        float2 vel = __ldg(vin + i);
+        if (ZB && (xb || y == 0 || y == g.H - 1)) vel = zero;
+        const float fx = (float)x - vel.x * dt * speed;
+        const float fy = (float)y - vel.y * dt * speed;
+        const Corners c = corners(fx, fy, g.W, g.H);
+        const int rl = c.lo_y * g.P, rh = c.hi_y * g.P;
+        float2 lt = __ldg(vin + rh + c.lo_x), rt = __ldg(vin + rh + c.hi_x);
+        float2 lb = __ldg(vin + rl + c.lo_x), rb = __ldg(vin + rl + c.hi_x);
+        if (ZB) {
+            const bool bxl = c.lo_x == 0 || c.lo_x == g.W - 1;
+            const bool bxh = c.hi_x == 0 || c.hi_x == g.W - 1;
+            const bool byl = c.lo_y == 0 || c.lo_y == g.H - 1;
+            const bool byh = c.hi_y == 0 || c.hi_y == g.H - 1;
+            if (bxl || byh) lt = zero;
+            if (bxh || byh) rt = zero;
+            if (bxl || byl) lb = zero;
+            if (bxh || byl) rb = zero;
+        }
+        const float h1x = mixf(lt.x, rt.x, c.dx), h1y = mixf(lt.y, rt.y, c.dx);
+        const float h2x = mixf(lb.x, rb.x, c.dx), h2y = mixf(lb.y, rb.y, c.dx);
+        const float sx = mixf(h2x, h1x, c.dy), sy = mixf(h2y, h1y, c.dy);
+        vout[i] = make_float2(clampf(sx * diss, -1.0f, 1.0f), clampf(sy * diss, -1.0f, 1.0f));
+    }
 }
 
 __global__ void __launch_bounds__(BX* BY) k_calc_vorticity(const float2* __restrict__ v, float* __restrict__ w, Grid g) {
@@ -139,6 +183,37 @@ __global__ void __launch_bounds__(BX* BY) k_density_advect(const float* __restri
     NX_CELLS(cell_density_advect(rin, rout, gd, v, mask, gv, sp, x, y));
 }
 
+// Density and velocity grids of one power-of-two size: the matching velocity
+// position x / W * W is x exactly (both operations exact), so the velocity is
+// the cell's own and its obstacle test the cell's own (cell_density_advect's
+// arithmetic otherwise; see its cell-centre note for the -0 case).
+__global__ void __launch_bounds__(BX* BY)
+    k_density_advect_same(const float* __restrict__ rin, float* __restrict__ rout, Grid gd,
+                          const float2* __restrict__ v, const uint8_t* __restrict__ mask, Grid gv,
+                          const __grid_constant__ StepParams sp) {
+    pdl_enter();
+    const int x = blockIdx.x * BX + threadIdx.x;
+    if (x >= gd.W) return;
+    const bool mz = sp.mask_zero != 0;
+    const float dt = sp.dt, speed = sp.d_speed, diss = sp.d_dissipation;
+    const int y0 = blockIdx.y * (BY * CPT) + threadIdx.y;
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+        const int y = y0 + k * BY;
+        if (y >= gd.H) break;
+        const int i = y * gd.P + x, vi = y * gv.P + x;
+        if (!mz && mask[vi]) {
+            rout[i] = 0.0f;
+            continue;
+        }
+        const float2 u = __ldg(v + vi);
+        const float fx = (float)x - u.x * dt * speed;
+        const float fy = (float)y - u.y * dt * speed;
+        const Corners c = corners(fx, fy, gd.W, gd.H);
+        rout[i] = sample_scalar(rin, gd.P, c) * diss;
+    }
+}
+
 // Vorticity confinement in one pass: shader.CalcVorticity.comp then
 // shader.ApplyVorticity.comp on a 32 x 16 output tile.  The block stages the
 // velocity of the tile plus 2 cells (index-clamped, as GetNeighbours reads),
@@ -163,7 +238,7 @@ __global__ void __launch_bounds__(BX* BY)
     for (int i = tid; i < VV_H * VV_W; i += BX * BY) {
         const int ry = i / VV_W, rx = i % VV_W;
         const int gx = min(max(x0 - 2 + rx, 0), g.W - 1), gy = min(max(y0 - 2 + ry, 0), g.H - 1);
-        sv[ry][rx] = __ldg(vin + (size_t)gy * g.P + gx);
+        sv[ry][rx] = __ldg(vin + gy * g.P + gx);
     }
     __syncthreads();
     for (int i = tid; i < VW_H * VW_W; i += BX * BY) {
@@ -191,14 +266,16 @@ __global__ void __launch_bounds__(BX* BY)
         float fy = 0.5f * (fabsf(wr) - fabsf(wl));
         const float d = fx * fx + fy * fy;
         const float m = eps > d ? eps : d;
-        const float rs = 1.0f / sqrtf(m);
+        // 1/sqrt(m) with both operations correctly rounded, as sqrtf and the
+        // IEEE division give (m >= eps is normal)
+        const float rs = __frcp_rn(__fsqrt_rn(m));
         fx = fx * rs;
         fy = fy * rs;
         const float s = vort * wc;
         fx = fx * (s * 1.0f);
         fy = fy * (s * -1.0f);
         const float2 v = sv[ty + 2][tx + 2];
-        const size_t c = (size_t)y * g.P + x;
+        const int c = y * g.P + x;
         vout[c] = make_float2(v.x + fx * dt, v.y + fy * dt);
         w[c] = wc;
     }
@@ -527,7 +604,7 @@ cudaError_t launch_obstacles(uint8_t* mask, Grid g, const ShapeOp* ops, int n, i
 }
 
 cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const ForceOp* ops,
-                           int n, cudaStream_t st) {
+                           int n, int zero_border, cudaStream_t st) {
     if (n < 0 || n > kMaxOpsPerLaunch) return cudaErrorInvalidValue;
     Grid gg = vel ? gv : gd;
     if (vel && rho) gg = Grid{gv.W > gd.W ? gv.W : gd.W, gv.H > gd.H ? gv.H : gd.H, 0};
@@ -535,18 +612,21 @@ cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const Forc
     const bool pdl = pdl_enabled();
     if (n <= 16)
         return launch_kernel(pdl, k_forcing<16>, grid, dim3(BX, BY), 0, st, vel, gv, rho, gd,
-                             op_block<ForceOp, 16>(ops, n));
+                             op_block<ForceOp, 16>(ops, n), zero_border);
     if (n <= 64)
         return launch_kernel(pdl, k_forcing<64>, grid, dim3(BX, BY), 0, st, vel, gv, rho, gd,
-                             op_block<ForceOp, 64>(ops, n));
+                             op_block<ForceOp, 64>(ops, n), zero_border);
     return launch_kernel(pdl, k_forcing<kMaxOpsPerLaunch>, grid, dim3(BX, BY), 0, st, vel, gv,
-                         rho, gd, op_block<ForceOp, kMaxOpsPerLaunch>(ops, n));
+                         rho, gd, op_block<ForceOp, kMaxOpsPerLaunch>(ops, n), zero_border);
 }
 
 cudaError_t launch_advect(const float2* vin, float2* vout, const uint8_t* mask, Grid g,
-                          const StepParams& sp, cudaStream_t st) {
-    return launch_kernel(pdl_enabled(), k_advect, grid_cpt(g), dim3(BX, BY), 0, st, vin, vout,
-                         mask, g, sp);
+                          const StepParams& sp, bool border_zeroed, cudaStream_t st) {
+    if (sp.has_borders && !border_zeroed)
+        return launch_kernel(pdl_enabled(), k_advect<true>, grid_cpt(g), dim3(BX, BY), 0, st, vin,
+                             vout, mask, g, sp);
+    return launch_kernel(pdl_enabled(), k_advect<false>, grid_cpt(g), dim3(BX, BY), 0, st, vin,
+                         vout, mask, g, sp);
 }
 
 cudaError_t launch_calc_vorticity(const float2* v, float* w, Grid g, cudaStream_t st) {
@@ -598,6 +678,10 @@ cudaError_t launch_subtract_gradient(const float2* vin, float2* vout, const floa
 cudaError_t launch_density_advect(const float* rin, float* rout, Grid gd, const float2* v,
                                   const uint8_t* mask, Grid gv, const StepParams& sp,
                                   cudaStream_t st) {
+    const auto pow2 = [](int n) { return (n & (n - 1)) == 0; };
+    if (gd.W == gv.W && gd.H == gv.H && pow2(gd.W) && pow2(gd.H))
+        return launch_kernel(pdl_enabled(), k_density_advect_same, grid_cpt(gd), dim3(BX, BY), 0,
+                             st, rin, rout, gd, v, mask, gv, sp);
     return launch_kernel(pdl_enabled(), k_density_advect, grid_cpt(gd), dim3(BX, BY), 0, st, rin,
                          rout, gd, v, mask, gv, sp);
 }
