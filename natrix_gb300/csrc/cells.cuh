@@ -128,11 +128,21 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
                                               int by0, bool zero_border = false) {
     __shared__ ForceOp s_ops[kMaxOpsPerLaunch];
     __shared__ int s_kept[kMaxOpsPerLaunch];
+    const int x = bx0 + threadIdx.x;
+    // the velocity rows' loads go out before the op list is staged and culled
+    // (several DRAM reads in flight per thread while the block prologue runs)
+    float2 va[ROWS];
+    if (vel) {
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            const int y = by0 + threadIdx.y + r * BY;
+            if (x < gv.W && y < gv.H) va[r] = vel[(size_t)y * gv.P + x];
+        }
+    }
     const int tid = threadIdx.y * BX + threadIdx.x;
     for (int i = tid; i < n; i += BX * BY) s_ops[i] = ops[i];
     __syncthreads();
     const int bx1 = bx0 + BX - 1, by1 = by0 + BY * ROWS - 1;
-    const int x = bx0 + threadIdx.x;
     if (vel) {
         int first_vel = -1;
         for (int k = 0; k < n; ++k)
@@ -150,13 +160,6 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
                                       bx1, by0, by1);
             return false;
         });
-        // all rows' loads first (several DRAM reads in flight per thread)
-        float2 va[ROWS];
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) {
-            const int y = by0 + threadIdx.y + r * BY;
-            if (first_vel >= 0 && x < gv.W && y < gv.H) va[r] = vel[(size_t)y * gv.P + x];
-        }
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) {
             const int y = by0 + threadIdx.y + r * BY;

@@ -7,6 +7,8 @@
 // Compiled with -fmad=false: see common.cuh for the arithmetic contract.
 #include <climits>
 #include <cstdlib>
+#include <algorithm>
+#include <vector>
 
 #include "cells.cuh"
 
@@ -53,6 +55,25 @@ __global__ void __launch_bounds__(BX* BY)
     pdl_enter();
     block_forcing<FORCE_ROWS>(vel, gv, rho, gd, ob.op, ob.n, blockIdx.x * BX,
                               blockIdx.y * BY * FORCE_ROWS, zero_border != 0);
+}
+
+// Density-only forcing touches cells inside the ops' footprints only, so the
+// launch covers just the 32x32 blocks a conservative footprint box reaches
+// (block ids in the parameter block); the in-kernel cull is unchanged.
+constexpr int kMaxForceTiles = 2048;
+struct ForceTiles {
+    int n, tiles_x;
+    uint16_t id[kMaxForceTiles];
+};
+
+template <int CAP>
+__global__ void __launch_bounds__(BX* BY)
+    k_forcing_tiles(float* __restrict__ rho, Grid gd, const __grid_constant__ OpBlock<ForceOp, CAP> ob,
+                    const __grid_constant__ ForceTiles tl) {
+    pdl_enter();
+    const int t = tl.id[blockIdx.x];
+    block_forcing<FORCE_ROWS>(nullptr, Grid{}, rho, gd, ob.op, ob.n, (t % tl.tiles_x) * BX,
+                              (t / tl.tiles_x) * BY * FORCE_ROWS);
 }
 
 template <typename Op, int CAP>
@@ -603,9 +624,62 @@ cudaError_t launch_obstacles(uint8_t* mask, Grid g, const ShapeOp* ops, int n, i
                          op_block<ShapeOp, kMaxOpsPerLaunch>(ops, n), fresh);
 }
 
+// Blocks (BX x BY*FORCE_ROWS cells) a density op can reach: its footprint's
+// bounding box with two cells of margin (the in-kernel cull keeps one).
+// Returns false when the list would not fit (launch the full grid then).
+bool density_force_tiles(const ForceOp* ops, int n, Grid gd, ForceTiles* tl) {
+    const int th = BY * FORCE_ROWS;
+    const int tx = (gd.W + BX - 1) / BX, ty = (gd.H + th - 1) / th;
+    if ((long)tx * ty > 65536) return false;
+    std::vector<uint8_t> hit((size_t)tx * ty, 0);
+    for (int k = 0; k < n; ++k) {
+        const ForceOp& op = ops[k];
+        float reach;
+        int y_end = gd.H;
+        if (op.kind == FORCE_GAUSS)
+            reach = 3.0f * op.r;
+        else if (op.kind == FORCE_CONE_DENSITY) {
+            reach = op.r;
+            y_end = op.rows < gd.H ? op.rows : gd.H;
+        } else
+            continue;
+        if (!(reach >= 0.0f) || y_end <= 0) continue;
+        const double cx = (double)op.px * gd.W, cy = (double)op.py * gd.H, rr = (double)reach + 2.0;
+        const double fx0 = std::max(cx - rr, 0.0), fx1 = std::min(cx + rr, (double)(gd.W - 1));
+        const double fy0 = std::max(cy - rr, 0.0), fy1 = std::min(cy + rr, (double)(y_end - 1));
+        if (!(fx0 <= fx1) || !(fy0 <= fy1)) continue;
+        for (int j = (int)fy0 / th; j <= (int)fy1 / th; ++j)
+            for (int i = (int)fx0 / BX; i <= (int)fx1 / BX; ++i) hit[(size_t)j * tx + i] = 1;
+    }
+    tl->n = 0;
+    tl->tiles_x = tx;
+    for (size_t t = 0; t < hit.size(); ++t)
+        if (hit[t]) {
+            if (tl->n == kMaxForceTiles) return false;
+            tl->id[tl->n++] = (uint16_t)t;
+        }
+    return true;
+}
+
+template <int CAP>
+cudaError_t launch_density_tiles(float* rho, Grid gd, const ForceOp* ops, int n,
+                                 const ForceTiles& tl, cudaStream_t st) {
+    if (tl.n == 0) return cudaSuccess;
+    return launch_kernel(pdl_enabled(), k_forcing_tiles<CAP>, dim3(tl.n), dim3(BX, BY), 0, st,
+                         rho, gd, op_block<ForceOp, CAP>(ops, n), tl);
+}
+
 cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const ForceOp* ops,
                            int n, int zero_border, cudaStream_t st) {
     if (n < 0 || n > kMaxOpsPerLaunch) return cudaErrorInvalidValue;
+    if (!vel && rho) {
+        ForceTiles tl;
+        if (density_force_tiles(ops, n, gd, &tl)) {
+            if (n <= 16) return launch_density_tiles<16>(rho, gd, ops, n, tl, st);
+            if (n <= 64) return launch_density_tiles<64>(rho, gd, ops, n, tl, st);
+            return launch_density_tiles<kMaxOpsPerLaunch>(rho, gd, ops, n, tl, st);
+        }
+    }
     Grid gg = vel ? gv : gd;
     if (vel && rho) gg = Grid{gv.W > gd.W ? gv.W : gd.W, gv.H > gd.H ? gv.H : gd.H, 0};
     const dim3 grid((gg.W + BX - 1) / BX, (gg.H + BY * FORCE_ROWS - 1) / (BY * FORCE_ROWS));
