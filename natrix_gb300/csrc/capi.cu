@@ -16,6 +16,7 @@
 //                writes a fresh mask; until then kernels treat it as empty)
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -104,6 +105,10 @@ struct natrix_sim {
     std::vector<ForceOp> fq;
     std::vector<ShapeOp> sq;
     bool mask_reset_pending = true;  // the mask memory does not hold the current obstacles
+    // Blocks (kRasterBlock^2 cells) of the mask memory that may be non-zero;
+    // mask_dirty_all when that is unknown (triangles, uploads, views handed out).
+    std::vector<uint8_t> mask_dirty;
+    bool mask_dirty_all = true;
     bool last_step_mask_zero = true;
     bool stepped = false;
     cudaStream_t last_stream = nullptr;
@@ -179,13 +184,48 @@ cudaStream_t stream_of(natrix_sim* s, void* stream) {
     return st;
 }
 
-// Rasterise queued obstacle shapes.
+// Rasterise queued obstacle shapes.  Circles rasterise over the blocks they
+// reach plus, when the mask is reset, the blocks the previous shapes left
+// non-zero; the rest of the mask is already zero (or, without a reset,
+// already right).  Triangles and unknown mask contents take the full grid.
 int flush_shapes(natrix_sim* s, cudaStream_t st) {
+    const Grid g = s->g;
+    const int bx = (g.W + kRasterBlock - 1) / kRasterBlock, by = (g.H + kRasterBlock - 1) / kRasterBlock;
+    const size_t nb = (size_t)bx * by;
+    if (s->mask_dirty.size() != nb) {
+        s->mask_dirty.assign(nb, 0);
+        s->mask_dirty_all = true;
+    }
     size_t done = 0;
+    std::vector<uint8_t> cur;
+    std::vector<uint16_t> ids;
     while (done < s->sq.size()) {
         const int n = (int)std::min<size_t>(kMaxOpsPerLaunch, s->sq.size() - done);
-        NX_LAUNCH(s, launch_obstacles(s->mask, s->g, s->sq.data() + done, n,
-                                      s->mask_reset_pending ? 1 : 0, st));
+        const ShapeOp* ops = s->sq.data() + done;
+        const bool fresh = s->mask_reset_pending;
+        cur.assign(nb, 0);
+        const bool bounded = nb <= 65536 && shape_blocks(ops, n, g, cur.data());
+        bool full = !bounded || (fresh && s->mask_dirty_all);
+        if (!full) {
+            ids.clear();
+            for (size_t b = 0; b < nb && !full; ++b)
+                if (cur[b] || (fresh && s->mask_dirty[b])) {
+                    if ((int)ids.size() == kMaxRasterBlocks) full = true;
+                    else ids.push_back((uint16_t)b);
+                }
+        }
+        if (full)
+            NX_LAUNCH(s, launch_obstacles(s->mask, g, ops, n, fresh ? 1 : 0, st));
+        else if (!ids.empty())
+            NX_LAUNCH(s, launch_obstacles_blocks(s->mask, g, ops, n, fresh ? 1 : 0, ids.data(),
+                                                 (int)ids.size(), st));
+        if (fresh) {
+            s->mask_dirty = cur;
+            s->mask_dirty_all = !bounded;
+        } else {
+            for (size_t b = 0; b < nb; ++b) s->mask_dirty[b] |= cur[b];
+            s->mask_dirty_all = s->mask_dirty_all || !bounded;
+        }
         s->mask_reset_pending = false;
         done += n;
     }
@@ -286,6 +326,8 @@ int materialise_mask(natrix_sim* s, cudaStream_t st) {
     if (s->mask_reset_pending) {
         NX_CUDA(cudaMemsetAsync(s->mask, 0, (size_t)s->g.P * s->g.H, st));
         s->mask_reset_pending = false;
+        std::fill(s->mask_dirty.begin(), s->mask_dirty.end(), (uint8_t)0);
+        s->mask_dirty_all = false;
     }
     return NATRIX_OK;
 }
@@ -351,6 +393,10 @@ int natrix_create(int32_t width, int32_t height, natrix_sim** out) {
                     "allocating a %dx%d simulator: %s", width, height, cudaGetErrorString(e));
     }
     s->mask_reset_pending = false;  // the memset left a valid empty mask
+    s->mask_dirty.assign((size_t)((width + kRasterBlock - 1) / kRasterBlock) *
+                             ((height + kRasterBlock - 1) / kRasterBlock),
+                         0);
+    s->mask_dirty_all = false;
     const char* err = nullptr;
     if (!jacobi_encode_maps_for(&s->maps, jacobi_config(s->g), s->p[0], s->p[1], s->div,
                                 s->flags, s->g, &err)) {
@@ -532,6 +578,7 @@ int natrix_field(natrix_sim* s, int32_t field, void** dev_ptr, int64_t* pitch) {
         case NATRIX_FIELD_OBSTACLES:
             rc = materialise_mask(s, st);
             if (rc) return rc;
+            s->mask_dirty_all = true;  // the caller may write through the view
             *dev_ptr = s->mask;
             break;
         default: return fail(NATRIX_EINVAL, "unknown field id %d", field);
@@ -545,7 +592,10 @@ int natrix_upload(natrix_sim* s, int32_t field, const void* host, void* stream) 
     cudaStream_t st = stream_of(s, stream);
     int rc = flush_fluid(s, st);
     if (rc) return rc;
-    if (field == NATRIX_FIELD_OBSTACLES) s->mask_reset_pending = false;
+    if (field == NATRIX_FIELD_OBSTACLES) {
+        s->mask_reset_pending = false;
+        s->mask_dirty_all = true;
+    }
     return field_copy(s, field, nullptr, host, true, st);
 }
 

@@ -108,6 +108,19 @@ void sim_count_launches(natrix_sim* sim, int n);
 // `ops` is host memory (n <= kMaxOpsPerLaunch), copied into the launch.
 cudaError_t launch_obstacles(uint8_t* mask, Grid g, const ShapeOp* ops, int n, int fresh,
                              cudaStream_t st);
+// Obstacle rasters and density forcing work on blocks of kRasterBlock^2 cells
+// (row-major block ids); a launch over listed blocks takes at most
+// kMaxRasterBlocks of them.
+constexpr int kRasterBlock = 32;
+constexpr int kMaxRasterBlocks = 2048;
+// Mark in hit[] (zeroed by the caller, one byte per block) every block a
+// circle of ops[0..n) can mark (bounding box, two cells of margin); false if
+// a shape cannot be bounded (a triangle: never culled).
+bool shape_blocks(const ShapeOp* ops, int n, Grid g, uint8_t* hit);
+// The raster of launch_obstacles restricted to blocks ids[0..n_ids); the
+// caller guarantees the mask is already right (zero when `fresh`) elsewhere.
+cudaError_t launch_obstacles_blocks(uint8_t* mask, Grid g, const ShapeOp* ops, int n, int fresh,
+                                    const uint16_t* ids, int n_ids, cudaStream_t st);
 // zero_border: also write the velocity grid's border cells as zero after the
 // ops (takes effect when the list holds a velocity op).
 cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const ForceOp* ops,

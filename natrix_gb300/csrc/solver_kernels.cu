@@ -60,11 +60,24 @@ __global__ void __launch_bounds__(BX* BY)
 // Density-only forcing touches cells inside the ops' footprints only, so the
 // launch covers just the 32x32 blocks a conservative footprint box reaches
 // (block ids in the parameter block); the in-kernel cull is unchanged.
-constexpr int kMaxForceTiles = 2048;
+static_assert(BX == kRasterBlock && BY * FORCE_ROWS == kRasterBlock, "raster block geometry");
 struct ForceTiles {
     int n, tiles_x;
-    uint16_t id[kMaxForceTiles];
+    uint16_t id[kMaxRasterBlocks];
 };
+
+// Obstacle raster over listed blocks only (the host keeps the mask zero
+// outside the blocks it lists).
+template <int CAP>
+__global__ void __launch_bounds__(BX* BY)
+    k_obstacles_blocks(uint8_t* __restrict__ mask, Grid g,
+                       const __grid_constant__ OpBlock<ShapeOp, CAP> ob, int fresh,
+                       const __grid_constant__ ForceTiles tl) {
+    pdl_enter();
+    const int t = tl.id[blockIdx.x];
+    block_obstacles<FORCE_ROWS>(mask, g, ob.op, ob.n, fresh, (t % tl.tiles_x) * BX,
+                                (t / tl.tiles_x) * BY * FORCE_ROWS);
+}
 
 template <int CAP>
 __global__ void __launch_bounds__(BX* BY)
@@ -101,16 +114,29 @@ __global__ void __launch_bounds__(BX* BY)
     const bool xb = ZB && (x == 0 || x == g.W - 1);
     const float2 zero = make_float2(0.0f, 0.0f);
     const int y0 = blockIdx.y * (BY * CPT) + threadIdx.y;
+    // every cell's own velocity and obstacle byte first (loads in flight
+    // together instead of one cell's chain after another)
+    float2 vc[CPT];
+    bool ob[CPT];
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+        const int y = y0 + k * BY;
+        const int i = y * g.P + x;
+        if (y < g.H) {
+            vc[k] = __ldg(vin + i);
+            ob[k] = !mz && mask[i];
+        }
+    }
 #pragma unroll
     for (int k = 0; k < CPT; ++k) {
         const int y = y0 + k * BY;
         if (y >= g.H) break;
         const int i = y * g.P + x;
-        if (!mz && mask[i]) {
+        if (ob[k]) {
             vout[i] = zero;
             continue;
         }
-        float2 vel = __ldg(vin + i);
+        float2 vel = vc[k];
         if (ZB && (xb || y == 0 || y == g.H - 1)) vel = zero;
         const float fx = (float)x - vel.x * dt * speed;
         const float fy = (float)y - vel.y * dt * speed;
@@ -218,16 +244,27 @@ __global__ void __launch_bounds__(BX* BY)
     const bool mz = sp.mask_zero != 0;
     const float dt = sp.dt, speed = sp.d_speed, diss = sp.d_dissipation;
     const int y0 = blockIdx.y * (BY * CPT) + threadIdx.y;
+    float2 uc[CPT];
+    bool ob[CPT];
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+        const int y = y0 + k * BY;
+        const int vi = y * gv.P + x;
+        if (y < gd.H) {
+            uc[k] = __ldg(v + vi);
+            ob[k] = !mz && mask[vi];
+        }
+    }
 #pragma unroll
     for (int k = 0; k < CPT; ++k) {
         const int y = y0 + k * BY;
         if (y >= gd.H) break;
-        const int i = y * gd.P + x, vi = y * gv.P + x;
-        if (!mz && mask[vi]) {
+        const int i = y * gd.P + x;
+        if (ob[k]) {
             rout[i] = 0.0f;
             continue;
         }
-        const float2 u = __ldg(v + vi);
+        const float2 u = uc[k];
         const float fx = (float)x - u.x * dt * speed;
         const float fy = (float)y - u.y * dt * speed;
         const Corners c = corners(fx, fy, gd.W, gd.H);
@@ -655,7 +692,7 @@ bool density_force_tiles(const ForceOp* ops, int n, Grid gd, ForceTiles* tl) {
     tl->tiles_x = tx;
     for (size_t t = 0; t < hit.size(); ++t)
         if (hit[t]) {
-            if (tl->n == kMaxForceTiles) return false;
+            if (tl->n == kMaxRasterBlocks) return false;
             tl->id[tl->n++] = (uint16_t)t;
         }
     return true;
@@ -667,6 +704,45 @@ cudaError_t launch_density_tiles(float* rho, Grid gd, const ForceOp* ops, int n,
     if (tl.n == 0) return cudaSuccess;
     return launch_kernel(pdl_enabled(), k_forcing_tiles<CAP>, dim3(tl.n), dim3(BX, BY), 0, st,
                          rho, gd, op_block<ForceOp, CAP>(ops, n), tl);
+}
+
+bool shape_blocks(const ShapeOp* ops, int n, Grid g, uint8_t* hit) {
+    const int tx = (g.W + kRasterBlock - 1) / kRasterBlock;
+    for (int k = 0; k < n; ++k) {
+        const ShapeOp& op = ops[k];
+        if (op.kind != SHAPE_CIRCLE) return false;  // triangles are never culled
+        // a cell is marked when its distance to the centre is <= r
+        if (!(op.a[2] >= 0.0f)) continue;
+        const double cx = (double)op.a[0] * g.W, cy = (double)op.a[1] * g.H;
+        const double rr = (double)op.a[2] + 2.0;
+        const double fx0 = std::max(cx - rr, 0.0), fx1 = std::min(cx + rr, (double)(g.W - 1));
+        const double fy0 = std::max(cy - rr, 0.0), fy1 = std::min(cy + rr, (double)(g.H - 1));
+        if (!(fx0 <= fx1) || !(fy0 <= fy1)) continue;
+        for (int j = (int)fy0 / kRasterBlock; j <= (int)fy1 / kRasterBlock; ++j)
+            for (int i = (int)fx0 / kRasterBlock; i <= (int)fx1 / kRasterBlock; ++i)
+                hit[(size_t)j * tx + i] = 1;
+    }
+    return true;
+}
+
+cudaError_t launch_obstacles_blocks(uint8_t* mask, Grid g, const ShapeOp* ops, int n, int fresh,
+                                    const uint16_t* ids, int n_ids, cudaStream_t st) {
+    if (n < 0 || n > kMaxOpsPerLaunch || n_ids < 0 || n_ids > kMaxRasterBlocks)
+        return cudaErrorInvalidValue;
+    if (n_ids == 0) return cudaSuccess;
+    ForceTiles tl;
+    tl.n = n_ids;
+    tl.tiles_x = (g.W + kRasterBlock - 1) / kRasterBlock;
+    for (int i = 0; i < n_ids; ++i) tl.id[i] = ids[i];
+    const bool pdl = pdl_enabled();
+    if (n <= 16)
+        return launch_kernel(pdl, k_obstacles_blocks<16>, dim3(n_ids), dim3(BX, BY), 0, st, mask, g,
+                             op_block<ShapeOp, 16>(ops, n), fresh, tl);
+    if (n <= 64)
+        return launch_kernel(pdl, k_obstacles_blocks<64>, dim3(n_ids), dim3(BX, BY), 0, st, mask, g,
+                             op_block<ShapeOp, 64>(ops, n), fresh, tl);
+    return launch_kernel(pdl, k_obstacles_blocks<kMaxOpsPerLaunch>, dim3(n_ids), dim3(BX, BY), 0,
+                         st, mask, g, op_block<ShapeOp, kMaxOpsPerLaunch>(ops, n), fresh, tl);
 }
 
 cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const ForceOp* ops,
