@@ -277,7 +277,8 @@ int run_jacobi(natrix_sim* s, int sweeps, cudaStream_t st) {
     while (sweeps > 0) {
         const int k = sweeps < per ? sweeps : per;
         NX_LAUNCH(s, launch_jacobi(s->d_maps, s->maps.config, s->p, s->p_cur, s->g, k,
-                                   s->d_marks[s->marks_cur], s->d_status, st));
+                                   s->d_marks[s->marks_cur], launches > 0 ? 1 : 0, s->d_status,
+                                   st));
         s->p_cur ^= 1;
         sweeps -= k;
         ++launches;

@@ -111,6 +111,14 @@ __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
+// The two halves, for kernels that order them the other way round: a grid
+// that triggers only after its own wait lets its successor start only once
+// the grid before it has completed.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Whether step launches use programmatic dependent launch (on unless the
 // environment sets NATRIX_PDL=0).
 bool pdl_enabled();

@@ -107,6 +107,10 @@ struct GridJobs {
     Grid g;
     int sweeps, tiles_x, n, tx, ty;
     const uint32_t* slow;  // tiles next to obstacles (TileMarks bits), or null
+    // Divergence, flags and marks were final before this launch's predecessor
+    // grid started (it is a sweep launch of the same chain): the first tile's
+    // divergence and flags may be fetched before the dependency wait.
+    int static_ready;
     __device__ __forceinline__ TileJob operator()(int t) const {
         return TileJob{p, d, f, pout, g, sweeps, (t % tiles_x) * tx, (t / tiles_x) * ty};
     }
@@ -119,6 +123,9 @@ constexpr int kMaxCtaTiles = 16;
 template <class Jobs>
 __device__ __forceinline__ const uint32_t* slow_marks(const Jobs&) { return nullptr; }
 __device__ __forceinline__ const uint32_t* slow_marks(const GridJobs& j) { return j.slow; }
+template <class Jobs>
+__device__ __forceinline__ bool static_ready(const Jobs&) { return false; }
+__device__ __forceinline__ bool static_ready(const GridJobs& j) { return j.static_ready != 0; }
 
 // Balanced deal of n tiles to G CTAs, computed by one warp for CTA b.  Order:
 // the marked (slow) tiles, then the others, each in index order; position p
@@ -314,13 +321,28 @@ using RtA = RtCfg<8, 16, 8>;
 // 16 warps x 9 rows: 128x144 region, 112x128 output tile
 using RtB = RtCfg<9, 16, 8>;
 
+// The three copies of a tile on one mbarrier phase: the expected bytes are
+// registered first, so the phase cannot complete before the last copy lands
+// even when the pressure copy is issued later (issue_pressure_load).
+template <class C>
+__device__ __forceinline__ void issue_static_loads(unsigned char* smem, uint64_t* bar,
+                                                   const TileJob& job) {
+    mbar_expect_tx(bar, 2 * C::P_BYTES + C::F_BYTES);
+    tma_load_2d(smem + C::OFF_D, job.d, job.tile_x - C::HXP, job.tile_y - C::HALO, bar);
+    tma_load_2d(smem + C::OFF_F, job.f, job.tile_x - C::HXF, job.tile_y - C::HALO, bar);
+}
+
+template <class C>
+__device__ __forceinline__ void issue_pressure_load(unsigned char* smem, uint64_t* bar,
+                                                    const TileJob& job) {
+    tma_load_2d(smem + C::OFF_P, job.p, job.tile_x - C::HXP, job.tile_y - C::HALO, bar);
+}
+
 template <class C>
 __device__ __forceinline__ void issue_tile_loads(unsigned char* smem, uint64_t* bar,
                                                  const TileJob& job) {
-    mbar_expect_tx(bar, 2 * C::P_BYTES + C::F_BYTES);
-    tma_load_2d(smem + C::OFF_P, job.p, job.tile_x - C::HXP, job.tile_y - C::HALO, bar);
-    tma_load_2d(smem + C::OFF_D, job.d, job.tile_x - C::HXP, job.tile_y - C::HALO, bar);
-    tma_load_2d(smem + C::OFF_F, job.f, job.tile_x - C::HXF, job.tile_y - C::HALO, bar);
+    issue_static_loads<C>(smem, bar, job);
+    issue_pressure_load<C>(smem, bar, job);
 }
 
 template <class C, class Jobs>
@@ -339,7 +361,12 @@ __global__ void __launch_bounds__(C::THREADS, 1)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int c0 = lane * 4, r0 = w * R;
 
-    pdl_enter();
+    // Programmatic dependent launch: wait, then trigger (a successor starts
+    // only after every CTA here has passed its wait).  When the static inputs
+    // are final the deal and the first tile's divergence / flags copies run
+    // before the wait.
+    const bool early = static_ready(jobs);
+    if (!early) pdl_wait();
     // this CTA's tiles: the balanced deal when the tiles are marked, else
     // blockIdx.x + k * gridDim.x
     __shared__ int s_tiles[kMaxCtaTiles];
@@ -361,12 +388,22 @@ __global__ void __launch_bounds__(C::THREADS, 1)
     auto tile_of = [&](int k) {
         return balanced ? s_tiles[k] : (int)blockIdx.x + k * (int)gridDim.x;
     };
-    if (n_mine == 0) return;
+    if (n_mine == 0) {
+        if (early) pdl_wait();
+        pdl_trigger();
+        return;
+    }
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
         fence_barrier_init();
-        issue_tile_loads<C>(smem, bar, jobs(tile_of(0)));
+        const TileJob first = jobs(tile_of(0));
+        issue_static_loads<C>(smem, bar, first);
+        if (early) pdl_wait();
+        issue_pressure_load<C>(smem, bar, first);
+    } else if (early) {
+        pdl_wait();
     }
+    pdl_trigger();
     uint32_t parity = 0;
     for (int k = 0; k < n_mine; ++k, parity ^= 1u) {
         const TileJob job = jobs(tile_of(k));
@@ -648,13 +685,14 @@ bool jacobi_encode_maps_for(JacobiMaps* maps, int config, float* p0, float* p1, 
 }
 
 cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbuf[2], int src,
-                          Grid g, int sweeps, const uint32_t* slow, int* status, cudaStream_t st) {
+                          Grid g, int sweeps, const uint32_t* slow, int static_ready, int* status,
+                          cudaStream_t st) {
     if (sweeps < 1 || sweeps > jacobi_max_sweeps_per_launch()) return cudaErrorInvalidValue;
     int tx, ty;
     jacobi_tile(config, &tx, &ty);
     const int tiles_x = (g.W + tx - 1) / tx, tiles_y = (g.H + ty - 1) / ty;
     const GridJobs jobs{&d_maps->p[src], &d_maps->div, &d_maps->flags, pbuf[1 - src], g,
-                        sweeps, tiles_x, tiles_x * tiles_y, tx, ty, slow};
+                        sweeps, tiles_x, tiles_x * tiles_y, tx, ty, slow, static_ready ? 1 : 0};
     const bool pdl = pdl_enabled();
     if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st, pdl);
     if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st, pdl);

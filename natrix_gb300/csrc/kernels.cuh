@@ -206,8 +206,11 @@ bool jacobi_encode_maps_for(JacobiMaps* maps, int config, float* p0, float* p1, 
 // `sweeps` (1..max) Jacobi sweeps of one grid from pbuf[src] into pbuf[1 - src];
 // `d_maps` is the device copy of the grid's maps.
 // `slow` (device, may be null) holds the tile marks of the current step.
+// static_ready: the previous launch on `st` is a sweep launch of the same
+// grid (divergence, flags and marks are final before it starts).
 cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbuf[2], int src,
-                          Grid g, int sweeps, const uint32_t* slow, int* status, cudaStream_t st);
+                          Grid g, int sweeps, const uint32_t* slow, int static_ready, int* status,
+                          cudaStream_t st);
 // One batched launch: every item is one tile of one simulation (device arrays).
 cudaError_t launch_jacobi_batch(int config, const JacobiBatchItem* items, int n_items,
                                 const JacobiBatchSim* sims, int* status, cudaStream_t st);
