@@ -7,7 +7,7 @@
 //     X[pixel + offset(t), c] * Wp[n, t, c]
 // M = 128 pixels of one image row, N = output channels, K = 9 * C.
 //
-// One persistent CTA per SM, ten warps, walking "segments": S consecutive
+// One persistent CTA per SM, eleven warps, walking "segments": S consecutive
 // output rows of one 128-pixel column strip of one image.  A segment's input
 // rows stream through a ring of R stages of G rows each (G = 4, 2 or 1, as
 // shared memory and TMEM allow); every input row is loaded once and serves
@@ -21,7 +21,8 @@
 //                  from x0 - 1, G rows} per 8-channel chunk (out-of-image
 //                  pixels, rows and channels read as zero, which is the
 //                  padding);
-//   warp 1 lane 0  MMA issuer: per step, G output rows x 9 taps x C/16
+//   warp 1 lane 0 and warp 10 lane 0  MMA issuers: per step, G output rows
+//                  (split between the two when G >= 2) x 9 taps x C/16
 //                  tcgen05.mma (K = 16 each) into the step's accumulator
 //                  slot (G accumulators of N columns; 2 to 4 slots in TMEM);
 //                  descriptors are precomputed bases plus offsets;
@@ -58,7 +59,8 @@ namespace {
 constexpr int kMaxStages = 32;
 constexpr int kMaxSlots = 4;     // TMEM accumulator slots (steps in flight past the MMA)
 constexpr int kEpiGroups = 2;    // epilogue groups of 4 warps
-constexpr int kThreads = 32 * (2 + 4 * kEpiGroups);
+constexpr int kIssuer2Warp = 2 + 4 * kEpiGroups;  // the second MMA issuer
+constexpr int kThreads = 32 * (3 + 4 * kEpiGroups);
 constexpr int kTileM = 128;
 constexpr int kBoxW = 136;                   // pixels per box: x0 - 1 .. x0 + 128, padded
 constexpr int kChunkBytes = 8 * kBoxW * 2;   // one 8-channel row: 2176 B
@@ -126,17 +128,18 @@ struct RingPos {
     }
 };
 
-// One step's MMAs: G output rows x 9 taps x PAIRS (16-channel K slices),
-// fully unrolled so every descriptor is a base plus a compile-time offset.
-// Rows past the segment's end are computed too (their input rows are staged
-// and their accumulators exist); the epilogue does not store them.
-template <int G, int PAIRS>
+// One issuer's share of a step's MMAs: output rows [RB, RB + RC) of the G,
+// x 9 taps x PAIRS (16-channel K slices), fully unrolled so every descriptor
+// is a base plus a compile-time offset.  Rows past the segment's end are
+// computed too (their input rows are staged and their accumulators exist);
+// the epilogue does not store them.
+template <int G, int RB, int RC, int PAIRS>
 __device__ __forceinline__ void issue_step(uint32_t d0, uint32_t n_cols, const uint32_t* soff,
                                            uint64_t a_base, uint64_t b_base, uint32_t a_pair,
                                            uint32_t b_pair, uint32_t b_tap, uint32_t idesc) {
     constexpr uint32_t kRow16 = kChunkBytes >> 4;
 #pragma unroll
-    for (int r = 0; r < G; ++r) {
+    for (int r = RB; r < RB + RC; ++r) {
         const uint32_t d = d0 + (uint32_t)r * n_cols;
 #pragma unroll
         for (int dy = 0; dy < 3; ++dy) {
@@ -163,6 +166,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         acc_empty[kMaxSlots], wbar;
     __shared__ uint32_t tmem_slot;
     constexpr int kLastExtra = G >= 2 ? 1 : 2;  // stages past t that step t reads
+    // MMA issuers: two threads (warps 1 and kIssuer2Warp) split a step's rows
+    // when G >= 2 (separate accumulators, so no ordering between them); a
+    // stage is free and a slot ready after one commit from each
+    constexpr int NI = G >= 2 ? 2 : 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int chunks = P.ctot / 8;  // 8-channel chunks per input row
     const int c0_chunks = P.c0 / 8;
@@ -173,10 +180,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < P.stages; ++s) {
             umma::mbar_init(&full[s], 1);
-            umma::mbar_init(&empty[s], 1);
+            umma::mbar_init(&empty[s], NI);
         }
         for (int a = 0; a < P.n_slots; ++a) {
-            umma::mbar_init(&acc_full[a], 1);
+            umma::mbar_init(&acc_full[a], NI);
             umma::mbar_init(&acc_empty[a], 4);
         }
         umma::mbar_init(&wbar, 1);
@@ -221,7 +228,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         }
         if (!ok) atomicOr(P.status, 2);
-    } else if (warp == 1 && lane == 0) {
+    } else if ((warp == 1 || (warp == kIssuer2Warp && NI == 2)) && lane == 0) {
+        const int ii = warp == 1 ? 0 : 1;  // issuer index
         bool ok = umma::mbar_wait(&wbar, 0);
         const uint32_t idesc = umma::idesc_bf16_f32(kTileM, P.N);
         const uint32_t lbo_a = (uint32_t)G * kChunkBytes;
@@ -253,8 +261,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                     for (int e = 0; e <= kLastExtra; ++e, q.next(R)) soff[e] = q.i * stage16;
                 }
-                issue_step<G, PAIRS>(tmem + slot.i * (uint32_t)G * (uint32_t)P.N, (uint32_t)P.N, soff,
-                                     a_base, b_base, a_pair, b_pair, b_tap, idesc);
+                const uint32_t d0 = tmem + slot.i * (uint32_t)G * (uint32_t)P.N;
+                if (ii == 0)
+                    issue_step<G, 0, G / NI, PAIRS>(d0, (uint32_t)P.N, soff, a_base, b_base,
+                                                    a_pair, b_pair, b_tap, idesc);
+                else
+                    issue_step<G, G / NI, G / NI, PAIRS>(d0, (uint32_t)P.N, soff, a_base, b_base,
+                                                         a_pair, b_pair, b_tap, idesc);
                 umma::commit(&acc_full[slot.i]);
                 // stage t has no later reader in this segment
                 umma::commit(&empty[st.i]);
@@ -267,7 +280,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             wt = q;  // every stage up to here was waited for
         }
         if (!ok) atomicOr(P.status, 2);
-    } else if (warp >= 2) {
+    } else if (warp >= 2 && warp < kIssuer2Warp) {
         const int quarter = warp & 3;  // TMEM lanes this warp may read
         const int group = (warp - 2) >> 2;
         const int row = quarter * 32 + lane;
