@@ -36,13 +36,19 @@ struct Corners {
     float dx, dy;
 };
 
+// The reference clamps ceil / floor in float, then converts.  Rounding and
+// converting in one instruction (cvt.rpi / cvt.rmi: saturating, NaN -> 0),
+// then clamping the integer, gives the same index for every input: finite
+// values round to the same integer, +-inf and out-of-range values saturate
+// to the same edge, NaN becomes 0 as the float clamp makes it.
+__device__ __forceinline__ int clamp_index(int v, int hi) { return min(max(v, 0), hi); }
+
 __device__ __forceinline__ Corners corners(float fx, float fy, int W, int H) {
     Corners c;
-    const float bx = (float)(W - 1), by = (float)(H - 1);
-    c.hi_x = (int)clampf(ceilf(fx), 0.0f, bx);
-    c.hi_y = (int)clampf(ceilf(fy), 0.0f, by);
-    c.lo_x = (int)clampf(floorf(fx), 0.0f, bx);
-    c.lo_y = (int)clampf(floorf(fy), 0.0f, by);
+    c.hi_x = clamp_index(__float2int_ru(fx), W - 1);
+    c.hi_y = clamp_index(__float2int_ru(fy), H - 1);
+    c.lo_x = clamp_index(__float2int_rd(fx), W - 1);
+    c.lo_y = clamp_index(__float2int_rd(fy), H - 1);
     c.dx = fx - (float)c.lo_x;
     c.dy = fy - (float)c.lo_y;
     return c;
