@@ -461,24 +461,47 @@ __global__ void __launch_bounds__(32 * ST_WARPS)
     const bool live = c < g.W;
     const int cc = live ? c : g.W - 2;
     const unsigned FULL = 0xffffffffu;
+    const bool edge_l = lane == 0, edge_r = lane == 31 || cc + 2 >= g.W;
     auto prow = [&](int y) {
         y = min(max(y, 0), g.H - 1);
         return __ldg(reinterpret_cast<const float2*>(p + (size_t)y * g.P + cc));
     };
-    float2 up = prow(y0 - 1), mid = prow(y0);
+    // one row's own loads: velocity pair, flags pair, and the pressure one
+    // column beyond the warp on the edge lanes
+    struct RowIn {
+        float4 q;
+        uint16_t fw;
+        float lp, rp;
+    };
+    auto load_row = [&](int y) {
+        RowIn r;
+        const size_t row = (size_t)y * g.P;
+        r.q = *reinterpret_cast<const float4*>(vin + row + cc);
+        r.fw = *reinterpret_cast<const uint16_t*>(flags + row + cc);
+        r.lp = edge_l ? __ldg(p + row + max(cc - 1, 0)) : 0.0f;
+        r.rp = edge_r ? __ldg(p + row + min(cc + 2, g.W - 1)) : 0.0f;
+        return r;
+    };
     const int y1 = min(y0 + ST_ROWS, g.H);
+    // rows y0 - 1 .. y0 + 1 of pressure and row y0's own loads up front; each
+    // iteration then issues the next row's loads before computing its own
+    float2 up = prow(y0 - 1), mid = prow(y0), dn = prow(y0 + 1);
+    RowIn cur = load_row(y0);
     for (int y = y0; y < y1; ++y) {
-        const float2 dn = prow(y + 1);
+        float2 dn2 = dn;
+        RowIn nxt = cur;
+        if (y + 1 < y1) {
+            dn2 = prow(y + 2);
+            nxt = load_row(y + 1);
+        }
         const size_t row = (size_t)y * g.P;
         float lp = __shfl_up_sync(FULL, mid.y, 1);
         float rp = __shfl_down_sync(FULL, mid.x, 1);
-        if (lane == 0) lp = __ldg(p + row + max(cc - 1, 0));
-        if (lane == 31 || cc + 2 >= g.W) rp = __ldg(p + row + min(cc + 2, g.W - 1));
+        if (edge_l) lp = cur.lp;
+        if (edge_r) rp = cur.rp;
         if (live) {
-            const uint16_t fw = *reinterpret_cast<const uint16_t*>(flags + row + c);
-            const uint8_t f0 = (uint8_t)(fw & 0xff), f1 = (uint8_t)(fw >> 8);
-            const float4 q = *reinterpret_cast<const float4*>(vin + row + c);
-            float2 v0 = make_float2(q.x, q.y), v1 = make_float2(q.z, q.w);
+            const uint8_t f0 = (uint8_t)(cur.fw & 0xff), f1 = (uint8_t)(cur.fw >> 8);
+            float2 v0 = make_float2(cur.q.x, cur.q.y), v1 = make_float2(cur.q.z, cur.q.w);
             {
                 const float pc = mid.x;
                 const float x1 = (f0 & NB_L) ? pc : lp;
@@ -501,6 +524,8 @@ __global__ void __launch_bounds__(32 * ST_WARPS)
         }
         up = mid;
         mid = dn;
+        dn = dn2;
+        cur = nxt;
     }
 }
 
