@@ -74,18 +74,60 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """SM clock, its maximum and the clock-event reasons during the timed
+    region: every 5 ms through NVML (ctypes on the driver's libnvidia-ml,
+    read-only queries) from a thread, or every 200 ms from nvidia-smi when
+    NVML cannot be loaded."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits (nvml.h)
+    REASON_BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,
+                   "hw_thermal_slowdown": 0x40}
 
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
         self.path = None
+        self.rows = []  # NVML samples: (sm_mhz, max_mhz, reasons bitmask)
+        self.thread = None
+        self.stop = None
+        self.nvml = None
+
+    def _nvml_open(self):
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.gpu), ctypes.byref(h)) != 0:
+            lib.nvmlShutdown()
+            return None
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        return lib, h, reasons
+
+    def _poll(self):
+        lib, h, reasons = self.nvml
+        sm, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop.is_set():
+            if (lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm)) == 0 and
+                    lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0 and
+                    reasons(h, ctypes.byref(rs)) == 0):
+                self.rows.append((sm.value, mx.value, rs.value))
+            self.stop.wait(0.005)
 
     def __enter__(self):
+        import threading
+        try:
+            self.nvml = self._nvml_open()
+        except (OSError, AttributeError):
+            self.nvml = None
+        if self.nvml is not None:
+            self.stop = threading.Event()
+            self.thread = threading.Thread(target=self._poll, daemon=True)
+            self.thread.start()
+            return self
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
@@ -98,6 +140,10 @@ class ClockSampler:
         return self
 
     def __exit__(self, *exc):
+        if self.thread is not None:
+            self.stop.set()
+            self.thread.join(timeout=5)
+            self.nvml[0].nvmlShutdown()
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -106,6 +152,14 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.thread is not None:
+            if not self.rows:
+                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+            names = sorted(n for n, bit in self.REASON_BITS.items()
+                           if any(r[2] & bit for r in self.rows))
+            return {"sm_mhz": float(np.median([r[0] for r in self.rows])),
+                    "sm_max_mhz": float(max(r[1] for r in self.rows)), "reasons": names,
+                    "samples": len(self.rows), "source": "nvml"}
         if not self.path or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         rows = []
@@ -122,7 +176,7 @@ class ClockSampler:
         reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
-                "samples": len(rows)}
+                "samples": len(rows), "source": "nvidia-smi"}
 
 
 def make_spec(name: str) -> wl.Workload:
@@ -777,7 +831,8 @@ def run_unet_forward(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 500 for the 2048x2048 workload, else 50)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["natrix", "reference"], default="natrix")
     ap.add_argument("--workload", choices=["large", "small", "particles", "batch", "warmstart",
@@ -790,6 +845,8 @@ def main():
                     help="warmstart: seconds allowed per solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 500 if args.workload == "large" else 50
     if args.warmup < 3 and args.impl == "natrix":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.workload == "batch":
