@@ -357,7 +357,11 @@ def run_natrix(args, spec):
     jl = max(int(stats.timed_launches), 1)
     launch_ms = stats.jacobi_ms / jl
     sweeps_per_launch = stats.timed_sweeps / jl
-    alg_bytes = BYTES["jacobi_sweep"] * cells * sweeps_per_launch
+    # a phase whose last launch also subtracted the pressure gradient carries
+    # that kernel's bytes too
+    fused_per_launch = int(stats.timed_fused) / jl
+    alg_bytes = (BYTES["jacobi_sweep"] * sweeps_per_launch +
+                 BYTES["subtract_gradient"] * fused_per_launch) * cells
     achieved = alg_bytes / (launch_ms / 1e3) / 1e9
     traffic = load_traffic(spec)
 
@@ -389,7 +393,10 @@ def run_natrix(args, spec):
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_kind": peak_kind,
                          "launch_ms": launch_ms, "sweeps_per_launch": sweeps_per_launch,
-                         "bytes_model": "13 B per cell per sweep"},
+                         "bytes_model": ("13 B per cell per sweep, plus 21 B per cell for the "
+                                         "gradient subtraction fused into the last launch "
+                                         "of each step" if fused_per_launch else
+                                         "13 B per cell per sweep")},
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": cells * 4},
             "gpu_launches": launches,

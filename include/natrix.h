@@ -247,6 +247,7 @@ typedef struct natrix_stats {
     int64_t timed_launches;  /* Jacobi launches inside the timed phases */
     int64_t timed_sweeps;    /* sweeps inside the timed phases */
     double jacobi_ms;        /* device time of the timed phases (CUDA events) */
+    int64_t timed_fused;     /* timed phases whose last launch also subtracted the gradient */
 } natrix_stats;
 
 /* Bracket the Jacobi phase of every following step with CUDA events on the

@@ -47,7 +47,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("kernel_launches", ctypes.c_int64), ("jacobi_launches", ctypes.c_int64),
                 ("jacobi_sweeps", ctypes.c_int64), ("timed_phases", ctypes.c_int64),
                 ("timed_launches", ctypes.c_int64), ("timed_sweeps", ctypes.c_int64),
-                ("jacobi_ms", ctypes.c_double)]
+                ("jacobi_ms", ctypes.c_double),
+                ("timed_fused", ctypes.c_int64)]
 
 
 _vp = ctypes.c_void_p

@@ -116,6 +116,7 @@ struct natrix_sim {
     bool timing = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timed;  // recorded phases
     std::vector<std::pair<int, int>> timed_counts;            // launches, sweeps
+    std::vector<int> timed_fused;  // the phase's last launch also subtracted the gradient
 };
 
 struct natrix_density {
@@ -140,6 +141,7 @@ void drop_timing_events(natrix_sim* s) {
     }
     s->timed.clear();
     s->timed_counts.clear();
+    s->timed_fused.clear();
 }
 
 void free_sim(natrix_sim* s) {
@@ -264,8 +266,14 @@ int flush_density(natrix_density* d, cudaStream_t st) {
     return flush_force_list(d->fluid, d->fq, nullptr, Grid{}, d->rho[d->cur], d->g, st);
 }
 
-int run_jacobi(natrix_sim* s, int sweeps, cudaStream_t st) {
+// `sweeps` Jacobi sweeps in launches of sweeps_per_launch.  With vin / vout
+// the gradient subtraction rides on the last launch when that launch can
+// take it (register-tiled tiles, fewer sweeps than the halo); *fused says
+// whether it did.
+int run_jacobi(natrix_sim* s, int sweeps, cudaStream_t st, const float2* vin = nullptr,
+               float2* vout = nullptr, bool* fused = nullptr) {
     const int per = s->prm.sweeps_per_launch > 0 ? s->prm.sweeps_per_launch : default_sweeps();
+    if (fused) *fused = false;
     if (sweeps <= 0) return NATRIX_OK;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (s->timing) {
@@ -274,21 +282,27 @@ int run_jacobi(natrix_sim* s, int sweeps, cudaStream_t st) {
         NX_CUDA(cudaEventRecord(e0, st));
     }
     int launches = 0, total = sweeps;
+    bool fuse_last = false;
     while (sweeps > 0) {
         const int k = sweeps < per ? sweeps : per;
+        const bool last = k == sweeps;
+        fuse_last = last && vin && s->maps.config != JACOBI_TB && k < default_sweeps();
         NX_LAUNCH(s, launch_jacobi(s->d_maps, s->maps.config, s->p, s->p_cur, s->g, k,
-                                   s->d_marks[s->marks_cur], launches > 0 ? 1 : 0, s->d_status,
-                                   st));
+                                   s->d_marks[s->marks_cur], launches > 0 ? 1 : 0,
+                                   fuse_last ? vin : nullptr, fuse_last ? vout : nullptr,
+                                   s->d_status, st));
         s->p_cur ^= 1;
         sweeps -= k;
         ++launches;
     }
     s->stats.jacobi_launches += launches;
     s->stats.jacobi_sweeps += total;
+    if (fused) *fused = fuse_last;
     if (s->timing) {
         NX_CUDA(cudaEventRecord(e1, st));
         s->timed.emplace_back(e0, e1);
         s->timed_counts.emplace_back(launches, total);
+        s->timed_fused.push_back(fuse_last ? 1 : 0);
     }
     return NATRIX_OK;
 }
@@ -520,9 +534,12 @@ int natrix_step(natrix_sim* s, float dt, void* stream) {
     }
     NX_LAUNCH(s, launch_divergence(s->vel[cur], s->mask, s->div, s->flags, s->p[0], g, sp, tm, st));
     s->p_cur = 0;
-    rc = run_jacobi(s, s->prm.iterations - 1, st);
+    bool fused = false;
+    rc = run_jacobi(s, s->prm.iterations - 1, st, s->vel[cur], s->vel[0], &fused);
     if (rc) return rc;
-    NX_LAUNCH(s, launch_subtract_gradient(s->vel[cur], s->vel[0], s->p[s->p_cur], s->flags, g, st));
+    if (!fused)
+        NX_LAUNCH(s, launch_subtract_gradient(s->vel[cur], s->vel[0], s->p[s->p_cur], s->flags, g,
+                                              st));
     // clear obstacles (fluid_simulator.py:267-280), applied lazily
     s->mask_reset_pending = true;
     s->last_step_mask_zero = mask_zero;
@@ -645,6 +662,7 @@ int natrix_get_stats(natrix_sim* s, natrix_stats* out, int32_t reset) {
         s->stats.timed_phases += 1;
         s->stats.timed_launches += s->timed_counts[i].first;
         s->stats.timed_sweeps += s->timed_counts[i].second;
+        s->stats.timed_fused += s->timed_fused[i];
     }
     drop_timing_events(s);
     *out = s->stats;

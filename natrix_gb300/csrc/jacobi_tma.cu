@@ -96,6 +96,12 @@ struct TileJob {
     Grid g;
     int sweeps;
     int tile_x, tile_y;
+    // Gradient subtraction fused after the sweeps (shader.SubtractGradient.comp
+    // on the output tile, from the register-resident pressure): vout = vin -
+    // grad p.  Null: not fused.  Needs sweeps < HALO, so the pressure one cell
+    // beyond the output tile is still exact.
+    const float2* vin;
+    float2* vout;
 };
 
 // Jobs of one grid: tile t of a tiles_x-wide decomposition.
@@ -107,12 +113,15 @@ struct GridJobs {
     Grid g;
     int sweeps, tiles_x, n, tx, ty;
     const uint32_t* slow;  // tiles next to obstacles (TileMarks bits), or null
+    const float2* vin;     // fused gradient subtraction (see TileJob), or null
+    float2* vout;
     // Divergence, flags and marks were final before this launch's predecessor
     // grid started (it is a sweep launch of the same chain): the first tile's
     // divergence and flags may be fetched before the dependency wait.
     int static_ready;
     __device__ __forceinline__ TileJob operator()(int t) const {
-        return TileJob{p, d, f, pout, g, sweeps, (t % tiles_x) * tx, (t / tiles_x) * ty};
+        return TileJob{p, d, f, pout, g, sweeps, (t % tiles_x) * tx, (t / tiles_x) * ty,
+                       vin, vout};
     }
 };
 
@@ -180,7 +189,7 @@ struct BatchJobs {
         const JacobiBatchItem it = items[t];
         const JacobiBatchSim& s = sims[it.sim];
         return TileJob{&s.maps.p[it.src], &s.maps.div, &s.maps.flags, s.p[1 - it.src], s.g,
-                       it.sweeps, it.tile_x, it.tile_y};
+                       it.sweeps, it.tile_x, it.tile_y, nullptr, nullptr};
     }
 };
 
@@ -500,8 +509,77 @@ __global__ void __launch_bounds__(C::THREADS, 1)
             }
         }
 
-        // output tile: region rows [HALO, HALO + TY), columns [HXP, HXP + TX)
         const Grid& g = job.g;
+        if (job.vin) {
+            // Gradient subtraction on the output tile (cell_subtract_gradient's
+            // arithmetic): one more exchange of the warps' edge rows, then each
+            // output cell reads its four neighbours from registers.
+            float* xs = X + (job.sweeps & 1) * (C::NW * 2 * RX);
+            *reinterpret_cast<float4*>(xs + (w * 2 + 0) * RX + c0) =
+                make_float4(p[0][0], p[0][1], p[0][2], p[0][3]);
+            *reinterpret_cast<float4*>(xs + (w * 2 + 1) * RX + c0) =
+                make_float4(p[R - 1][0], p[R - 1][1], p[R - 1][2], p[R - 1][3]);
+            __syncthreads();
+            float up[4], below[4];
+            {
+                const float4 a =
+                    w > 0 ? *reinterpret_cast<const float4*>(xs + ((w - 1) * 2 + 1) * RX + c0)
+                          : make_float4(p[0][0], p[0][1], p[0][2], p[0][3]);
+                const float4 b =
+                    w < C::NW - 1
+                        ? *reinterpret_cast<const float4*>(xs + ((w + 1) * 2 + 0) * RX + c0)
+                        : make_float4(p[R - 1][0], p[R - 1][1], p[R - 1][2], p[R - 1][3]);
+                up[0] = a.x; up[1] = a.y; up[2] = a.z; up[3] = a.w;
+                below[0] = b.x; below[1] = b.y; below[2] = b.z; below[3] = b.w;
+            }
+            const bool out_col = c0 >= C::HXP && c0 < C::HXP + C::TX;
+            const int gx = job.tile_x + c0 - C::HXP;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                float cur[4], dn[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    cur[j] = p[r][j];
+                    dn[j] = r < R - 1 ? p[r + 1][j] : below[j];
+                }
+                const float lft = __shfl_up_sync(FULL, cur[3], 1);
+                const float rgt = __shfl_down_sync(FULL, cur[0], 1);
+                const int rr = r0 + r;
+                const int gy = job.tile_y + rr - C::HALO;
+                if (out_col && rr >= C::HALO && rr < C::HALO + C::TY && gy < g.H && gx < g.W) {
+                    const float L[4] = {lft, cur[0], cur[1], cur[2]};
+                    const float Rn[4] = {cur[1], cur[2], cur[3], rgt};
+                    const size_t o = (size_t)gy * g.P + gx;
+                    const float4 va = *reinterpret_cast<const float4*>(job.vin + o);
+                    const float4 vb = *reinterpret_cast<const float4*>(job.vin + o + 2);
+                    float2 v[4] = {make_float2(va.x, va.y), make_float2(va.z, va.w),
+                                   make_float2(vb.x, vb.y), make_float2(vb.z, vb.w)};
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const uint32_t fb = f[r] >> (8 * j);
+                        const float pc = cur[j];
+                        const float x1 = (fb & NB_L) ? pc : L[j];
+                        const float x2 = (fb & NB_R) ? pc : Rn[j];
+                        const float y1 = (fb & NB_B) ? pc : up[j];
+                        const float y2 = (fb & NB_T) ? pc : dn[j];
+                        v[j].x -= 0.5f * (x2 - x1);
+                        v[j].y -= 0.5f * (y2 - y1);
+                    }
+                    if (gx + 3 < g.W) {
+                        *reinterpret_cast<float4*>(job.vout + o) = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+                        *reinterpret_cast<float4*>(job.vout + o + 2) = make_float4(v[2].x, v[2].y, v[3].x, v[3].y);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            if (gx + j < g.W) job.vout[o + j] = v[j];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) up[j] = cur[j];
+            }
+        }
+
+        // output tile: region rows [HALO, HALO + TY), columns [HXP, HXP + TX)
         if (c0 >= C::HXP && c0 < C::HXP + C::TX) {
             const int gx = job.tile_x + c0 - C::HXP;
 #pragma unroll
@@ -685,14 +763,18 @@ bool jacobi_encode_maps_for(JacobiMaps* maps, int config, float* p0, float* p1, 
 }
 
 cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbuf[2], int src,
-                          Grid g, int sweeps, const uint32_t* slow, int static_ready, int* status,
-                          cudaStream_t st) {
+                          Grid g, int sweeps, const uint32_t* slow, int static_ready,
+                          const float2* vin, float2* vout, int* status, cudaStream_t st) {
     if (sweeps < 1 || sweeps > jacobi_max_sweeps_per_launch()) return cudaErrorInvalidValue;
+    // the fused gradient needs the register-tiled kernel and one valid halo cell
+    if (vin && (config == JACOBI_TB || sweeps >= jacobi_max_sweeps_per_launch()))
+        return cudaErrorInvalidValue;
     int tx, ty;
     jacobi_tile(config, &tx, &ty);
     const int tiles_x = (g.W + tx - 1) / tx, tiles_y = (g.H + ty - 1) / ty;
     const GridJobs jobs{&d_maps->p[src], &d_maps->div, &d_maps->flags, pbuf[1 - src], g,
-                        sweeps, tiles_x, tiles_x * tiles_y, tx, ty, slow, static_ready ? 1 : 0};
+                        sweeps, tiles_x, tiles_x * tiles_y, tx, ty, slow, vin, vout,
+                        static_ready ? 1 : 0};
     const bool pdl = pdl_enabled();
     if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st, pdl);
     if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st, pdl);

@@ -208,9 +208,12 @@ bool jacobi_encode_maps_for(JacobiMaps* maps, int config, float* p0, float* p1, 
 // `slow` (device, may be null) holds the tile marks of the current step.
 // static_ready: the previous launch on `st` is a sweep launch of the same
 // grid (divergence, flags and marks are final before it starts).
+// vin / vout (may be null): also subtract the pressure gradient, vout = vin -
+// grad p with the result's pressure (register-tiled configurations, sweeps
+// below the per-launch maximum).
 cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbuf[2], int src,
-                          Grid g, int sweeps, const uint32_t* slow, int static_ready, int* status,
-                          cudaStream_t st);
+                          Grid g, int sweeps, const uint32_t* slow, int static_ready,
+                          const float2* vin, float2* vout, int* status, cudaStream_t st);
 // One batched launch: every item is one tile of one simulation (device arrays).
 cudaError_t launch_jacobi_batch(int config, const JacobiBatchItem* items, int n_items,
                                 const JacobiBatchSim* sims, int* status, cudaStream_t st);
