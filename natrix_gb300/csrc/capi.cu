@@ -11,7 +11,8 @@
 //   [viscosity]  cur -> other          (only when viscosity > 0, as :219-228)
 //   divergence   cur -> div, flags, p = first sweep from zero
 //   jacobi       iterations-1 sweeps, `sweeps_per_launch` fused per launch
-//   subtract     cur, p -> vel0
+//   subtract     cur, p -> vel0 (inside the last Jacobi launch when that one
+//                has fewer sweeps than the tile halo, else its own launch)
 //   obstacle reset: recorded on the host, applied lazily (the next raster
 //                writes a fresh mask; until then kernels treat it as empty)
 #include <cuda_runtime.h>
