@@ -165,6 +165,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[kMaxSlots],
         acc_empty[kMaxSlots], wbar;
     __shared__ uint32_t tmem_slot;
+    // bias and 1x1-head weights, read by every epilogue thread for every
+    // pixel: staged once (N <= 128)
+    __shared__ __align__(16) float s_bias[128], s_head[128];
     constexpr int kLastExtra = G >= 2 ? 1 : 2;  // stages past t that step t reads
     // MMA issuers: two threads (warps 1 and kIssuer2Warp) split a step's rows
     // when G >= 2 (separate accumulators, so no ordering between them); a
@@ -190,6 +193,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         umma::mbar_init_fence();
     }
     if (warp == 1) umma::tmem_alloc(&tmem_slot, P.tmem_cols);
+    for (int i = threadIdx.x; i < P.N; i += blockDim.x) {
+        s_bias[i] = P.bias ? P.bias[i] : 0.0f;
+        s_head[i] = P.head_w ? P.head_w[i] : 0.0f;
+    }
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
@@ -312,9 +319,17 @@ __global__ void __launch_bounds__(kThreads, 1)
                         float v[16];
                         umma::tmem_ld16(tmem + lane_base + col0 + (uint32_t)c, v);
                         if (!inside) continue;
-                        if (P.bias)
+                        if (P.bias) {
+                            const float4* b4 = reinterpret_cast<const float4*>(s_bias + c);
 #pragma unroll
-                            for (int jj = 0; jj < 16; ++jj) v[jj] += P.bias[c + jj];
+                            for (int q = 0; q < 4; ++q) {
+                                const float4 b = b4[q];
+                                v[4 * q] += b.x;
+                                v[4 * q + 1] += b.y;
+                                v[4 * q + 2] += b.z;
+                                v[4 * q + 3] += b.w;
+                            }
+                        }
                         if (P.relu)
 #pragma unroll
                             for (int jj = 0; jj < 16; ++jj) v[jj] = v[jj] > 0.0f ? v[jj] : 0.0f;
@@ -328,9 +343,17 @@ __global__ void __launch_bounds__(kThreads, 1)
                                 if (!(bf16_to_f(h) > 0.0f)) v[jj] = 0.0f;
                             }
                         }
-                        if (P.head_out)
+                        if (P.head_out) {
+                            const float4* h4 = reinterpret_cast<const float4*>(s_head + c);
 #pragma unroll
-                            for (int jj = 0; jj < 16; ++jj) head += P.head_w[c + jj] * v[jj];
+                            for (int q = 0; q < 4; ++q) {
+                                const float4 hw = h4[q];
+                                head += hw.x * v[4 * q];
+                                head += hw.y * v[4 * q + 1];
+                                head += hw.z * v[4 * q + 2];
+                                head += hw.w * v[4 * q + 3];
+                            }
+                        }
                         uint32_t packed[8];
 #pragma unroll
                         for (int jj = 0; jj < 8; ++jj)
