@@ -128,12 +128,9 @@ cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const Forc
 // border_zeroed: vin's border cells already hold zero (no test on read).
 cudaError_t launch_advect(const float2* vin, float2* vout, const uint8_t* mask, Grid g,
                           const StepParams& sp, bool border_zeroed, cudaStream_t st);
-cudaError_t launch_calc_vorticity(const float2* v, float* w, Grid g, cudaStream_t st);
 // calc + apply in one pass (same results); writes the curl to w
 cudaError_t launch_vorticity(const float2* vin, float2* vout, float* w, Grid g,
                              const StepParams& sp, cudaStream_t st);
-cudaError_t launch_apply_vorticity(const float2* vin, float2* vout, const float* w, Grid g,
-                                   const StepParams& sp, cudaStream_t st);
 cudaError_t launch_viscosity(const float2* vin, float2* vout, Grid g, const StepParams& sp,
                              cudaStream_t st);
 // `marks` (may have a null `mark`) receives the tiles with obstacle rows.

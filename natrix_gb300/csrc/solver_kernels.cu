@@ -161,18 +161,6 @@ __global__ void __launch_bounds__(BX* BY)
     }
 }
 
-__global__ void __launch_bounds__(BX* BY) k_calc_vorticity(const float2* __restrict__ v, float* __restrict__ w, Grid g) {
-    pdl_enter();
-    NX_CELLS(cell_calc_vorticity(v, w, g, x, y));
-}
-
-__global__ void __launch_bounds__(BX* BY) k_apply_vorticity(const float2* __restrict__ vin, float2* __restrict__ vout,
-                      const float* __restrict__ w, Grid g, const __grid_constant__ StepParams spv) {
-    pdl_enter();
-    const StepParams* sp = &spv;
-    NX_CELLS(cell_apply_vorticity(vin, vout, w, g, sp, x, y));
-}
-
 __global__ void __launch_bounds__(BX* BY) k_viscosity(const float2* __restrict__ vin, float2* __restrict__ vout, Grid g,
                 const __grid_constant__ StepParams spv) {
     pdl_enter();
@@ -802,17 +790,6 @@ cudaError_t launch_advect(const float2* vin, float2* vout, const uint8_t* mask, 
                              vout, mask, g, sp);
     return launch_kernel(pdl_enabled(), k_advect<false>, grid_cpt(g), dim3(BX, BY), 0, st, vin,
                          vout, mask, g, sp);
-}
-
-cudaError_t launch_calc_vorticity(const float2* v, float* w, Grid g, cudaStream_t st) {
-    return launch_kernel(pdl_enabled(), k_calc_vorticity, grid_cpt(g), dim3(BX, BY), 0, st, v, w,
-                         g);
-}
-
-cudaError_t launch_apply_vorticity(const float2* vin, float2* vout, const float* w, Grid g,
-                                   const StepParams& sp, cudaStream_t st) {
-    return launch_kernel(pdl_enabled(), k_apply_vorticity, grid_cpt(g), dim3(BX, BY), 0, st, vin,
-                         vout, w, g, sp);
 }
 
 cudaError_t launch_vorticity(const float2* vin, float2* vout, float* w, Grid g,
