@@ -10,7 +10,8 @@ one frame: obstacles, forcing, FluidSimulator.update, SmoothParticlesArea.update
 
 One JSON line on rank 0.  `value` is timed with CUDA events on the launching
 stream with the fields resident on the device (the per-step forcing records,
-~1.5 KB, go through the API's pinned staging as they would for any caller).
+~1.5 KB, travel host->device inside the kernel launches' parameter blocks, as
+they do for any caller).
 `e2e` adds, every step, a device->host read of the density frame into pinned
 host memory through the C ABI (on a copy stream, overlapping the next step).  `roofline` is the Jacobi
 phase (the dominant kernel), timed live with CUDA events around its launches.
@@ -366,8 +367,9 @@ def run_natrix(args, spec):
     traffic = load_traffic(spec)
 
     if rank == 0:
-        # per-frame host->device bytes: splat records for velocity and density,
-        # obstacle shapes, two step-parameter blocks (sizes of the C structs)
+        # per-frame host->device bytes (carried in the launches' parameter
+        # blocks): splat records for velocity and density, obstacle shapes,
+        # two step-parameter blocks (sizes of the C structs)
         h2d = 32 * spec.splats_per_step * 2 + 32 * spec.n_obstacles + 48 * 2
         cpu = None
         if not args.no_cpu:
