@@ -456,14 +456,67 @@ __global__ void __launch_bounds__(C::THREADS, 1)
             issue_tile_loads<C>(smem, bar, jobs(tile_of(k + 1)));
         }
 
+        // One sweep of row r from the old values of the rows above (up) and
+        // below (dn); left / right neighbours by shuffle.
+        auto sweep_row = [&](int r, const float* up, const float* dn) {
+            float cur[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) cur[j] = p[r][j];
+            float lft = __shfl_up_sync(FULL, cur[3], 1);
+            float rgt = __shfl_down_sync(FULL, cur[0], 1);
+            lft = wall_l ? cur[0] : lft;
+            rgt = wall_r ? cur[3] : rgt;
+            const float L[4] = {lft, cur[0], cur[1], cur[2]};
+            const float Rn[4] = {cur[1], cur[2], cur[3], rgt};
+            if (slow & (1u << r)) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const uint32_t fb = f[r] >> (8 * j);
+                    const float l = (fb & NB_L) ? cur[j] : L[j];
+                    const float rr = (fb & NB_R) ? cur[j] : Rn[j];
+                    const float b = (fb & NB_B) ? cur[j] : up[j];
+                    const float tt = (fb & NB_T) ? cur[j] : dn[j];
+                    p[r][j] = (l + rr + b + tt - d[r][j]) * 0.25f;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    p[r][j] = (L[j] + Rn[j] + up[j] + dn[j] - d[r][j]) * 0.25f;
+            }
+        };
+        // Each sweep: publish the warp's edge rows, sweep the interior rows
+        // (their neighbours are this warp's own), then the CTA barrier, then
+        // the two edge rows with the neighbouring warps' rows.  Warps reach
+        // the barrier after the bulk of their work, so arrival skew costs
+        // less; rows 1 and R-2 keep their old values for the edge rows.
         for (int s = 0; s < job.sweeps; ++s) {
             float* xs = X + (s & 1) * (C::NW * 2 * RX);
             *reinterpret_cast<float4*>(xs + (w * 2 + 0) * RX + c0) =
                 make_float4(p[0][0], p[0][1], p[0][2], p[0][3]);
             *reinterpret_cast<float4*>(xs + (w * 2 + 1) * RX + c0) =
                 make_float4(p[R - 1][0], p[R - 1][1], p[R - 1][2], p[R - 1][3]);
+            float old1[4], oldm[4];  // rows 1 and R-2 before this sweep
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                old1[j] = p[1][j];
+                oldm[j] = p[R - 2][j];
+            }
+            {
+                float up[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) up[j] = p[0][j];
+#pragma unroll
+                for (int r = 1; r < R - 1; ++r) {
+                    float cur[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) cur[j] = p[r][j];
+                    sweep_row(r, up, p[r + 1]);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) up[j] = cur[j];
+                }
+            }
             __syncthreads();
-            float up[4], below[4];
+            float up0[4], belowR[4];
             {
                 const float4 a =
                     w > 0 ? *reinterpret_cast<const float4*>(xs + ((w - 1) * 2 + 1) * RX + c0)
@@ -472,43 +525,12 @@ __global__ void __launch_bounds__(C::THREADS, 1)
                     w < C::NW - 1
                         ? *reinterpret_cast<const float4*>(xs + ((w + 1) * 2 + 0) * RX + c0)
                         : make_float4(p[R - 1][0], p[R - 1][1], p[R - 1][2], p[R - 1][3]);
-                up[0] = a.x; up[1] = a.y; up[2] = a.z; up[3] = a.w;
-                below[0] = b.x; below[1] = b.y; below[2] = b.z; below[3] = b.w;
+                up0[0] = a.x; up0[1] = a.y; up0[2] = a.z; up0[3] = a.w;
+                belowR[0] = b.x; belowR[1] = b.y; belowR[2] = b.z; belowR[3] = b.w;
             }
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                float cur[4], dn[4];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    cur[j] = p[r][j];
-                    dn[j] = r < R - 1 ? p[r + 1][j] : below[j];
-                }
-                float lft = __shfl_up_sync(FULL, cur[3], 1);
-                float rgt = __shfl_down_sync(FULL, cur[0], 1);
-                lft = wall_l ? cur[0] : lft;
-                rgt = wall_r ? cur[3] : rgt;
-                const float L[4] = {lft, cur[0], cur[1], cur[2]};
-                const float Rn[4] = {cur[1], cur[2], cur[3], rgt};
-                if (slow & (1u << r)) {
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const uint32_t fb = f[r] >> (8 * j);
-                        const float l = (fb & NB_L) ? cur[j] : L[j];
-                        const float rr = (fb & NB_R) ? cur[j] : Rn[j];
-                        const float b = (fb & NB_B) ? cur[j] : up[j];
-                        const float tt = (fb & NB_T) ? cur[j] : dn[j];
-                        p[r][j] = (l + rr + b + tt - d[r][j]) * 0.25f;
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        p[r][j] = (L[j] + Rn[j] + up[j] + dn[j] - d[r][j]) * 0.25f;
-                }
-#pragma unroll
-                for (int j = 0; j < 4; ++j) up[j] = cur[j];
-            }
+            sweep_row(0, up0, old1);
+            sweep_row(R - 1, oldm, belowR);
         }
-
         const Grid& g = job.g;
         if (job.vin) {
             // Gradient subtraction on the output tile (cell_subtract_gradient's
