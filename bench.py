@@ -41,6 +41,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+from natrix_gb300 import replicas  # noqa: E402
 from natrix_gb300 import workloads as wl  # noqa: E402
 
 # Algorithmic bytes per cell (float2 velocity 8 B, float scalars 4 B, uint8
@@ -279,7 +280,7 @@ def run_natrix(args, spec):
     sim.iterations, sim.vorticity, sim.viscosity = spec.iterations, spec.vorticity, spec.viscosity
     sim.speed, sim.dissipation = spec.speed, spec.dissipation
     den.speed, den.dissipation = spec.speed, spec.dissipation
-    seed = rank
+    seed = replicas.replica_seed(rank)
     obst = wl.workload_obstacles(seed, spec)
     total = args.warmup + 2 * args.steps
     forcing = [wl.step_forcing(seed, i, spec) for i in range(total)]
@@ -346,12 +347,9 @@ def run_natrix(args, spec):
     barrier()
     sim.sync()
 
-    ms_t = torch.tensor([ms, t_e2e * 1e3], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms, ms_e2e = float(ms_t[0]), float(ms_t[1])
-    value = cells * args.steps * world / (ms / 1e3)
-    e2e_value = cells * args.steps * world / (ms_e2e / 1e3)
+    ms, ms_e2e = replicas.max_over_ranks([ms, t_e2e * 1e3], device="cuda")
+    value = replicas.whole_job_rate(cells * args.steps, world, ms / 1e3)
+    e2e_value = replicas.whole_job_rate(cells * args.steps, world, ms_e2e / 1e3)
 
     peak, peak_kind = load_peaks()
     step_b = step_bytes_per_cell(spec)
