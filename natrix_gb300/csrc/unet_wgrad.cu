@@ -42,9 +42,11 @@ __device__ __forceinline__ float bfw(uint16_t h) { return __uint_as_float((uint3
 // matrices along K and its SBO the chunk slot between core matrices along
 // M / N.  No register transposes: warp 0 lane 0 issues the TMA copies of a
 // stage (the 66-pixel x segments of every input chunk, the 64-pixel dZ
-// segments), warp 1 lane 0 issues the 3 x 4 MMAs of a chunk (M = 128 channel
-// rows, N = cout, K = 16 pixels) into the three accumulators of the pass,
-// warps 2-5 read the accumulators out after each pass.  Channel rows past
+// segments); warp 1 lane 0 and, when two accumulator sets fit in TMEM
+// (6 cout <= 512), warp 6 lane 0 issue the 3 x 4 MMAs of alternate chunks
+// (M = 128 channel rows, N = cout, K = 16 pixels) into their own three
+// accumulators of the pass; warps 2-5 read the accumulators out after each
+// pass and add the two sets.  Channel rows past
 // cin read whatever their chunk slots hold; those accumulator rows are never
 // read.
 
@@ -59,7 +61,8 @@ struct RingPos {
     }
 };
 
-constexpr int kMnThreads = 192;
+constexpr int kMnThreads = 224;
+constexpr int kIssuer2 = 6;  // warp of the second MMA issuer
 constexpr int kXSlot = 1152;                  // 66 pixels x 16 B, padded to 128 B
 constexpr int kZSlot = kChunkPix * 16;        // 64 pixels x 16 B
 constexpr int kASlots = kRowsA / 8;           // channel chunks of M = 128
@@ -73,6 +76,7 @@ struct WgMnParams {
     uint32_t tmem_cols;
     uint32_t stage_bytes;  // kASlots x kXSlot + cout / 8 x kZSlot
     int stages;
+    int issuers;  // 1 or 2 (two accumulator sets of 3 cout columns)
 };
 
 __global__ void __launch_bounds__(kMnThreads, 1)
@@ -94,7 +98,7 @@ __global__ void __launch_bounds__(kMnThreads, 1)
             umma::mbar_init(&full[i], 1);
             umma::mbar_init(&empty[i], 1);
         }
-        umma::mbar_init(&done, 1);
+        umma::mbar_init(&done, (uint32_t)P.issuers);
         umma::mbar_init_fence();
         s_ok = 1;
     }
@@ -129,7 +133,9 @@ __global__ void __launch_bounds__(kMnThreads, 1)
                     umma::tma_load_4d(st + a_bytes + q * kZSlot, &tdz, 8 * q, x0, y, b, &full[ps.i]);
             }
             if (!ok) s_ok = 0;
-        } else if (warp == 1 && lane == 0) {
+        } else if ((warp == 1 || (warp == kIssuer2 && P.issuers == 2)) && lane == 0) {
+            const int ii = warp == 1 ? 0 : 1;  // this issuer takes chunks it % issuers == ii
+            const uint32_t acc = tmem + (uint32_t)(ii * 3 * cout);
             // both operands MN-major (instruction descriptor bits 15, 16)
             const uint32_t idesc = umma::idesc_bf16_f32(kRowsA, cout) | (1u << 15) | (1u << 16);
             // MN-major without swizzling: LBO = 128 B between 8-pixel groups
@@ -138,7 +144,9 @@ __global__ void __launch_bounds__(kMnThreads, 1)
             const uint64_t b0 = umma::smem_desc(umma::smem_u32(smem + a_bytes), 128, kZSlot);
             const uint32_t stage16 = P.stage_bytes >> 4;
             int it = 0;
+            bool first = true;  // this issuer's first chunk of the pass
             for (int ch = ch0; ch < ch1 && ok; ++ch, ++it, ms.next(R)) {
+                if (it % P.issuers != ii) continue;
                 ok = umma::mbar_wait(&full[ms.i], ms.ph);
                 if (!ok) break;
                 umma::fence_after_sync();
@@ -147,16 +155,18 @@ __global__ void __launch_bounds__(kMnThreads, 1)
                 for (int dxi = 0; dxi < 3; ++dxi) {
 #pragma unroll
                     for (int m = 0; m < kChunkPix / 16; ++m)
-                        umma::mma_bf16(tmem + (uint32_t)(dxi * cout),
+                        umma::mma_bf16(acc + (uint32_t)(dxi * cout),
                                        ab + (uint32_t)dxi + (uint32_t)m * 16u,
                                        bb + (uint32_t)m * 16u, idesc,
-                                       (it > 0 || m > 0) ? 1u : 0u);
+                                       (!first || m > 0) ? 1u : 0u);
                 }
+                first = false;
                 umma::commit(&empty[ms.i]);
             }
+
             umma::commit(&done);
             if (!ok) s_ok = 0;
-        } else if (warp >= 2) {
+        } else if (warp >= 2 && warp < kIssuer2) {
             // the pass's accumulators: wait for the last commit, then read
             bool w = true;
             if (lane == 0) w = umma::mbar_wait(&done, (uint32_t)pass & 1u);
@@ -170,6 +180,16 @@ __global__ void __launch_bounds__(kMnThreads, 1)
                 for (int c = 0; c < 3 * cout; c += 16) {
                     float v[16];
                     umma::tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
+                    // the second set holds a sum only when the second issuer
+                    // had a chunk (the block has at least two)
+                    if (P.issuers == 2 && ch1 - ch0 >= 2) {
+                        float v2[16];
+                        umma::tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) +
+                                            (uint32_t)(3 * cout + c),
+                                        v2);
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) v[j] += v2[j];
+                    }
                     if (ci < cin) {
 #pragma unroll
                         for (int j = 0; j < 16; ++j) {
@@ -275,8 +295,9 @@ int wgrad_tc(const uint16_t* dz, int cout, const uint16_t* x0, int c0, const uin
     P.n_chunks = B * H * P.cpr;
     P.dw = dw;
     P.status = status;
+    P.issuers = 6 * cout <= 512 ? 2 : 1;
     uint32_t cols = 32;
-    while (cols < (uint32_t)(3 * cout)) cols *= 2;
+    while (cols < (uint32_t)(3 * cout * P.issuers)) cols *= 2;
     P.tmem_cols = cols;
     P.stage_bytes = (uint32_t)kASlots * kXSlot + (uint32_t)(cout / 8) * kZSlot;
     const uint32_t budget = 200u * 1024u;
