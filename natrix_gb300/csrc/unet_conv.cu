@@ -213,6 +213,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         RingPos ps;
         bool ok = true;
+        // stages armed and the parity of each one's last lap: the copies must
+        // land before the CTA exits, even after a wait ran out
+        uint32_t armed = 0, armed_ph = 0;
         for (int u = blockIdx.x; u < P.n_units && ok; u += gridDim.x) {
             const Unit U = unit_of(P, u);
             const int x0 = U.tx * kTileM;
@@ -225,6 +228,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                 }
                 umma::mbar_arrive_expect_tx(&full[ps.i], P.stage_bytes);
+                armed |= 1u << ps.i;
+                armed_ph = (armed_ph & ~(1u << ps.i)) | (ps.ph << ps.i);
                 unsigned char* d = smem + P.smem_a + ps.i * P.stage_bytes;
                 for (int q = 0; q < chunks; ++q, d += G * kChunkBytes) {
                     if (q < c0_chunks || c1_chunks == 0)
@@ -235,6 +240,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         }
         if (!ok) atomicOr(P.status, 2);
+        for (uint32_t i = 0; i < R; ++i)
+            if ((armed >> i) & 1u) umma::mbar_wait(&full[i], (armed_ph >> i) & 1u);
     } else if ((warp == 1 || (warp == kIssuer2Warp && NI == 2)) && lane == 0) {
         const int ii = warp == 1 ? 0 : 1;  // issuer index
         bool ok = umma::mbar_wait(&wbar, 0);

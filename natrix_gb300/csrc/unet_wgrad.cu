@@ -112,6 +112,9 @@ __global__ void __launch_bounds__(kMnThreads, 1)
     const int ch0 = blockIdx.x * per;
     const int ch1 = min(ch0 + per, P.n_chunks);
     RingPos ps, ms;  // producer / MMA positions in the stage ring (continue across passes)
+    // stages the producer has armed, and the parity of each one's last lap:
+    // before the CTA exits it waits for those copies to land
+    uint32_t armed = 0, armed_ph = 0;
     bool ok = true;
 
     for (int pass = 0; pass < 3 && ch0 < ch1; ++pass) {
@@ -124,6 +127,8 @@ __global__ void __launch_bounds__(kMnThreads, 1)
                 const int y = row % P.H, b = row / P.H;
                 unsigned char* st = smem + ps.i * P.stage_bytes;
                 umma::mbar_arrive_expect_tx(&full[ps.i], tx_bytes);
+                armed |= 1u << ps.i;
+                armed_ph = (armed_ph & ~(1u << ps.i)) | (ps.ph << ps.i);
                 for (int q = 0; q < q0; ++q)
                     umma::tma_load_4d(st + q * kXSlot, &tx0, 8 * q, x0 - 1, y + dy, b, &full[ps.i]);
                 for (int q = 0; q < q1; ++q)
@@ -208,7 +213,14 @@ __global__ void __launch_bounds__(kMnThreads, 1)
             break;
         }
     }
-    if (tid == 0 && (!ok || !s_ok)) atomicOr(P.status, 4);
+    if (tid == 0) {
+        // every copy this CTA issued has landed before it exits (on a normal
+        // run these phases completed long ago; after a wait ran out they may
+        // still be in flight)
+        for (uint32_t i = 0; i < R; ++i)
+            if ((armed >> i) & 1u) umma::mbar_wait(&full[i], (armed_ph >> i) & 1u);
+        if (!ok || !s_ok) atomicOr(P.status, 4);
+    }
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 1) umma::tmem_dealloc(tmem, P.tmem_cols);
@@ -303,6 +315,12 @@ int wgrad_tc(const uint16_t* dz, int cout, const uint16_t* x0, int c0, const uin
     const uint32_t budget = 200u * 1024u;
     P.stages = (int)(budget / P.stage_bytes);
     if (P.stages > kMnMaxStages) P.stages = kMnMaxStages;
+    // Two issuers take alternate chunks; with an even ring every stage's
+    // chunks share one parity, so each stage is only ever consumed by one
+    // issuer, lap after lap in order.  (With an odd ring an issuer could wait
+    // for a stage's next lap before the current lap had landed, and the
+    // parity test would match the lap before.)
+    if (P.issuers == 2 && (P.stages & 1)) --P.stages;
     if (P.stages < 2) return wg_fail(NATRIX_EINVAL, "wgrad: stage does not fit");
     // slack past the last stage: every descriptor read stays inside the
     // allocation whichever of its two strides runs along K
