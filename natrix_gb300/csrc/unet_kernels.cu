@@ -336,16 +336,30 @@ __global__ void __launch_bounds__(256)
     float accb = 0.0f;
 #pragma unroll
     for (int c = 0; c < 16; ++c) acc[c] = 0.0f;
+    float w[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) w[c] = hw[c];
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
          i += (long)gridDim.x * blockDim.x) {
         const float g = dp[i];
         accb += g;
+        // the pixel's 16 channels: two 16-byte loads and two 16-byte stores
+        const uint4* src = reinterpret_cast<const uint4*>(d1 + i * 16);
+        const uint4 u0 = src[0], u1 = src[1];
+        const uint32_t in[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+        uint32_t out[8];
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-            const float a = bf(d1[i * 16 + c]);
-            acc[c] += g * a;
-            dz[i * 16 + c] = a > 0.0f ? tobf(g * hw[c]) : (uint16_t)0;
+        for (int k = 0; k < 8; ++k) {
+            const float a0 = bf((uint16_t)(in[k] & 0xffffu)), a1 = bf((uint16_t)(in[k] >> 16));
+            acc[2 * k] += g * a0;
+            acc[2 * k + 1] += g * a1;
+            const uint16_t z0 = a0 > 0.0f ? tobf(g * w[2 * k]) : (uint16_t)0;
+            const uint16_t z1 = a1 > 0.0f ? tobf(g * w[2 * k + 1]) : (uint16_t)0;
+            out[k] = (uint32_t)z0 | ((uint32_t)z1 << 16);
         }
+        uint4* dst = reinterpret_cast<uint4*>(dz + i * 16);
+        dst[0] = make_uint4(out[0], out[1], out[2], out[3]);
+        dst[1] = make_uint4(out[4], out[5], out[6], out[7]);
     }
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
@@ -394,9 +408,9 @@ __global__ void __launch_bounds__(256)
     const int b = blockIdx.y;
     const size_t pb = (size_t)b * H * W, mb = (size_t)b * H * P;
     double acc[5] = {0, 0, 0, 0, 0};
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < (long)H * W;
-         i += (long)gridDim.x * blockDim.x) {
-        const int x = (int)(i % W), y = (int)(i / W);
+    const int hw = H * W;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < hw; i += gridDim.x * blockDim.x) {
+        const int y = i / W, x = i - y * W;
         if (mask && mask[mb + (size_t)y * P + x]) continue;
         const float e = p[pb + i] - target[pb + i];
         const float bb = div[mb + (size_t)y * P + x] * inv_scale[b];
@@ -413,23 +427,22 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// residual r on fluid cells (0 elsewhere), for the gradient of the residual term
+// residual r on fluid cells (0 elsewhere), for the gradient of the residual
+// term; blockIdx.y is the image
 __global__ void k_loss_resid(const float* __restrict__ p, const float* __restrict__ div,
                              const float* __restrict__ inv_scale, const uint8_t* __restrict__ mask,
                              int B, int H, int W, int P, float* __restrict__ r) {
-    const long n = (long)B * H * W;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-         i += (long)gridDim.x * blockDim.x) {
-        const int b = (int)(i / ((long)H * W));
-        const long k = i % ((long)H * W);
-        const int x = (int)(k % W), y = (int)(k / W);
-        const size_t pb = (size_t)b * H * W, mb = (size_t)b * H * P;
+    const int b = blockIdx.y, hw = H * W;
+    const size_t pb = (size_t)b * hw, mb = (size_t)b * H * P;
+    const float scale = inv_scale[b];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < hw; k += gridDim.x * blockDim.x) {
+        const int y = k / W, x = k - y * W;
         if (mask && mask[mb + (size_t)y * P + x]) {
-            r[i] = 0.0f;
+            r[pb + k] = 0.0f;
             continue;
         }
-        const float bb = div[mb + (size_t)y * P + x] * inv_scale[b];
-        r[i] = bb - apply_op(p, pb, mask, mb, x, y, W, H, P);
+        const float bb = div[mb + (size_t)y * P + x] * scale;
+        r[pb + k] = bb - apply_op(p, pb, mask, mb, x, y, W, H, P);
     }
 }
 
@@ -439,24 +452,25 @@ __global__ void k_loss_grad(const float* __restrict__ p, const float* __restrict
                             const float* __restrict__ r, const uint8_t* __restrict__ mask,
                             const double* __restrict__ sums, float lambda, int B, int H, int W,
                             int P, float* __restrict__ dp) {
-    const long n = (long)B * H * W;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-         i += (long)gridDim.x * blockDim.x) {
-        const int b = (int)(i / ((long)H * W));
-        const long k = i % ((long)H * W);
-        const int x = (int)(k % W), y = (int)(k / W);
-        const size_t pb = (size_t)b * H * W, mb = (size_t)b * H * P;
+    // blockIdx.y is the image; its constants once per thread, not per pixel
+    const int b = blockIdx.y, hw = H * W;
+    const size_t pb = (size_t)b * hw, mb = (size_t)b * H * P;
+    const double* s = sums + b * 6;
+    const double nf = s[0] > 0 ? s[0] : 1.0;
+    const float mean_e = (float)(s[1] / nf);
+    const float c1 = (float)(2.0 / (B * nf));
+    const float c2 = -lambda * (float)(2.0 / (B * (s[4] > 0 ? s[4] : 1.0)));
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < hw; k += gridDim.x * blockDim.x) {
+        const int y = k / W, x = k - y * W;
+        const size_t i = pb + k;
         if (mask && mask[mb + (size_t)y * P + x]) {
             dp[i] = 0.0f;
             continue;
         }
-        const double* s = sums + b * 6;
-        const double nf = s[0] > 0 ? s[0] : 1.0;
-        const float mean_e = (float)(s[1] / nf);
         const float e = p[i] - target[i] - mean_e;
-        const float g1 = (float)(2.0 / (B * nf)) * e;
+        const float g1 = c1 * e;
         const float ar = apply_op(r, pb, mask, mb, x, y, W, H, P);
-        const float g2 = -lambda * (float)(2.0 / (B * (s[4] > 0 ? s[4] : 1.0))) * ar;
+        const float g2 = c2 * ar;
         dp[i] = g1 + g2;
     }
 }
@@ -656,11 +670,10 @@ int natrix_nn_loss(const float* p, const float* target, const float* div, const 
     const long per = (long)H * W;
     const unsigned bx = blocks(per, 256) < 256 ? blocks(per, 256) : 256;
     k_loss_sums<<<dim3(bx, B), 256, 0, st>>>(p, target, div, inv_scale, mask, H, W, P, sums);
-    const long n = (long)B * per;
-    const unsigned g = blocks(n, 256) < 8192 ? blocks(n, 256) : 8192;
     if (dp) {
-        k_loss_resid<<<g, 256, 0, st>>>(p, div, inv_scale, mask, B, H, W, P, r);
-        k_loss_grad<<<g, 256, 0, st>>>(p, target, r, mask, sums, lambda, B, H, W, P, dp);
+        const unsigned gx = blocks(per, 256) < 1024 ? blocks(per, 256) : 1024;
+        k_loss_resid<<<dim3(gx, B), 256, 0, st>>>(p, div, inv_scale, mask, B, H, W, P, r);
+        k_loss_grad<<<dim3(gx, B), 256, 0, st>>>(p, target, r, mask, sums, lambda, B, H, W, P, dp);
     }
     return launch_status();
 }
