@@ -407,23 +407,37 @@ __global__ void __launch_bounds__(256)
                 double* __restrict__ sums /* B x 6: n, se, see, srr, sbb, pad */) {
     const int b = blockIdx.y;
     const size_t pb = (size_t)b * H * W, mb = (size_t)b * H * P;
-    double acc[5] = {0, 0, 0, 0, 0};
+    // per-thread partial sums in FP32 over the thread's few pixels (the grid
+    // gives each thread about four), then FP64 for the reductions
+    float fa[5] = {0, 0, 0, 0, 0};
     const int hw = H * W;
+    const float scale = inv_scale[b];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < hw; i += gridDim.x * blockDim.x) {
         const int y = i / W, x = i - y * W;
         if (mask && mask[mb + (size_t)y * P + x]) continue;
         const float e = p[pb + i] - target[pb + i];
-        const float bb = div[mb + (size_t)y * P + x] * inv_scale[b];
+        const float bb = div[mb + (size_t)y * P + x] * scale;
         const float r = bb - apply_op(p, pb, mask, mb, x, y, W, H, P);
-        acc[0] += 1.0;
-        acc[1] += e;
-        acc[2] += (double)e * e;
-        acc[3] += (double)r * r;
-        acc[4] += (double)bb * bb;
+        fa[0] += 1.0f;
+        fa[1] += e;
+        fa[2] += e * e;
+        fa[3] += r * r;
+        fa[4] += bb * bb;
     }
+    // warp sums, then the block's, then one atomic per block and value (the
+    // images' 5 sums are few addresses shared by every block of the image)
+    __shared__ double part[8][5];
+    const int warp = threadIdx.x >> 5;
+#pragma unroll
     for (int j = 0; j < 5; ++j) {
-        const double v = warp_sum_d(acc[j]);
-        if ((threadIdx.x & 31) == 0) atomicAdd(sums + b * 6 + j, v);
+        const double v = warp_sum_d((double)fa[j]);
+        if ((threadIdx.x & 31) == 0) part[warp][j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w][threadIdx.x];
+        atomicAdd(sums + b * 6 + threadIdx.x, t);
     }
 }
 
@@ -452,14 +466,19 @@ __global__ void k_loss_grad(const float* __restrict__ p, const float* __restrict
                             const float* __restrict__ r, const uint8_t* __restrict__ mask,
                             const double* __restrict__ sums, float lambda, int B, int H, int W,
                             int P, float* __restrict__ dp) {
-    // blockIdx.y is the image; its constants once per thread, not per pixel
+    // blockIdx.y is the image; its constants (FP64 divisions) once per block
     const int b = blockIdx.y, hw = H * W;
     const size_t pb = (size_t)b * hw, mb = (size_t)b * H * P;
-    const double* s = sums + b * 6;
-    const double nf = s[0] > 0 ? s[0] : 1.0;
-    const float mean_e = (float)(s[1] / nf);
-    const float c1 = (float)(2.0 / (B * nf));
-    const float c2 = -lambda * (float)(2.0 / (B * (s[4] > 0 ? s[4] : 1.0)));
+    __shared__ float s_c[3];
+    if (threadIdx.x == 0) {
+        const double* s = sums + b * 6;
+        const double nf = s[0] > 0 ? s[0] : 1.0;
+        s_c[0] = (float)(s[1] / nf);
+        s_c[1] = (float)(2.0 / (B * nf));
+        s_c[2] = -lambda * (float)(2.0 / (B * (s[4] > 0 ? s[4] : 1.0)));
+    }
+    __syncthreads();
+    const float mean_e = s_c[0], c1 = s_c[1], c2 = s_c[2];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < hw; k += gridDim.x * blockDim.x) {
         const int y = k / W, x = k - y * W;
         const size_t i = pb + k;
