@@ -787,6 +787,186 @@ def run_unet_train(args):
     }), flush=True)
 
 
+def run_aux(args):
+    """The kernels outside the default step, each at a full working size and
+    timed with CUDA events over --steps calls after --warmup, so that every
+    kernel of the library has a measured bandwidth (ncu launch lists of this
+    workload give the per-kernel split):
+
+    * on a 2048x2048 system after 5 steps of the large workload's settings:
+      the FP64 residual (natrix_residual: two launches and a 40-byte read-back
+      with a host wait per call), the per-region residual
+      (natrix_residual_regions), the allocation-free residual
+      (natrix_residual_noalloc), 80 Jacobi sweeps (natrix_jacobi, 10 launches
+      of 8; NATRIX_JACOBI_VARIANT=0 selects the shared-memory sweep kernel)
+      and a step with viscosity 0.1 (its extra launch, against one without);
+    * the FP64 conjugate-gradient kernels on 16 x 512 x 512;
+    * Adam over the warm-start network's parameters, with the bf16 repack;
+    * the integer cells of 4M particles (natrix_particles_cells, with the
+      32 MB read-back into pinned host memory).
+
+    Algorithmic bytes per cell or element (each input read once, each output
+    written once): residual 10 (pressure, divergence, mask, flags), per-region
+    residual 13 (pressure, divergence, flags, label), allocation-free 9
+    (pressure, divergence, mask), sweep launch 13, CG apply 17 (direction 8,
+    mask 1, product 8), dot 17, axpy 24, direction update 24, Adam 28 per
+    parameter (weight, gradient, two moments read; weight and moments
+    written)."""
+    import torch
+
+    from natrix_gb300 import _lib
+    from natrix_gb300.core import warmstart as ws
+    from natrix_gb300.core.particles import LagrangianParticles
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    hbm, kind = load_peaks()
+    lib = _lib.load()
+
+    def timed(fn, n=None):
+        n = n or args.steps
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    kernels = {}
+
+    def report(name, ms, nbytes, launches, note=None):
+        gbs = nbytes / ms / 1e6
+        kernels[name] = {"us_per_call": ms * 1e3, "bytes": nbytes, "launches_per_call": launches,
+                         "gbs": gbs, "frac": gbs / hbm}
+        if note:
+            kernels[name]["note"] = note
+
+    # 2048x2048 solver system
+    N = 2048
+    sim, mask = ws.evaluation_system(N, seed=7)
+    cells = N * N
+    regions = ws.Regions(mask.view(1, N, -1), 1, N, N)
+    labels, n_labels = regions.image_labels(0)
+    sums = torch.empty(n_labels, 5, dtype=torch.float64, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p, div = sim.pressure, sim.divergence
+    pitch = p.stride(0)
+    dmask = torch.zeros(N, pitch, dtype=torch.uint8, device="cuda")
+    dmask[:, :N] = mask.view(N, -1)[:, :N]
+    out5 = torch.empty(5, dtype=torch.float64, device="cuda")
+
+    report("residual", timed(sim.residual_sums), 10.0 * cells, 2,
+           "per call: k_residual, k_residual_final, 40-byte read-back, host wait")
+
+    def regions_call():
+        _lib.check(lib.natrix_residual_regions(sim.handle, ctypes.c_void_p(labels.data_ptr()),
+                                               n_labels, ctypes.c_void_p(sums.data_ptr()), st))
+
+    report("residual_regions", timed(regions_call), 13.0 * cells, 1,
+           f"k_residual_labels over {n_labels} regions (plus a memset of the sums)")
+
+    def noalloc_call():
+        _lib.check(lib.natrix_residual_noalloc(ctypes.c_void_p(p.data_ptr()),
+                                               ctypes.c_void_p(div.data_ptr()),
+                                               ctypes.c_void_p(dmask.data_ptr()), N, N, pitch,
+                                               ctypes.c_void_p(out5.data_ptr()), st))
+
+    report("residual_noalloc", timed(noalloc_call), 9.0 * cells, 2,
+           "k_residual_noalloc, k_residual_noalloc_final")
+    variant = "shared-memory (k_jacobi_tb)" if os.environ.get("NATRIX_JACOBI_VARIANT") == "0" \
+        else "register-tiled (k_jacobi_rt)"
+    report("jacobi_80_sweeps", timed(lambda: sim.jacobi(80)), 10 * 13.0 * cells, 10,
+           f"{variant}, 10 launches of 8 sweeps")
+
+    rng = np.random.default_rng(11)
+
+    def step():
+        sim.add_splats(wl.gauss_splats(rng, 16, N, N, 5.0))
+        sim.update(1 / 60)
+
+    plain_ms = timed(step)
+    sim.viscosity = 0.1
+    viscous_ms = timed(step)
+    sim.viscosity = 0.0
+    report("viscosity", max(viscous_ms - plain_ms, 1e-6), 16.0 * cells, 1,
+           f"step with viscosity 0.1 ({viscous_ms:.4f} ms) minus without ({plain_ms:.4f} ms); "
+           "k_viscosity reads and writes the velocity")
+    sim.sync()
+
+    # FP64 conjugate-gradient kernels, 16 x 512 x 512
+    B, H, W = 16, 512, 512
+    P = (W + 31) // 32 * 32
+    g = torch.Generator(device="cuda").manual_seed(0)
+    m = (torch.rand(B, H, P, device="cuda", generator=g) < 0.05).to(torch.uint8)
+    d = torch.randn(B, H, W, dtype=torch.float64, device="cuda", generator=g)
+    r = torch.randn_like(d)
+    x = torch.zeros_like(d)
+    q = torch.empty_like(d)
+    rr = torch.ones(B, dtype=torch.float64, device="cuda")
+    rr2, dq = torch.ones_like(rr), torch.ones_like(rr)
+    per, n_el = H * W, B * H * W
+    P_ = ws._p
+    S = ws._s
+    report("cg_apply", timed(lambda: ws._call("natrix_nn_cg_apply", P_(d), P_(m), B, H, W, P,
+                                              P_(q), S())), 17.0 * n_el, 1)
+    report("cg_dot", timed(lambda: ws._call("natrix_nn_cg_dot", P_(d), P_(q), P_(m), B, H, W, P,
+                                            P_(dq), S())), 17.0 * n_el, 1,
+           "FP64 sums per image")
+    # axpy adds +-rr/dq times the direction: alternate the sign so x stays bounded
+    report("cg_axpy", timed(lambda: (ws._call("natrix_nn_cg_axpy", P_(x), P_(d), P_(rr), P_(dq),
+                                              1.0, B, per, S()),
+                                     ws._call("natrix_nn_cg_axpy", P_(x), P_(d), P_(rr), P_(dq),
+                                              -1.0, B, per, S()))) / 2, 24.0 * n_el, 1)
+    report("cg_dir", timed(lambda: ws._call("natrix_nn_cg_dir", P_(d), P_(r), P_(rr2), P_(rr), B,
+                                            per, S())), 24.0 * n_el, 1,
+           "direction = r + (rr_new / rr) direction, with rr_new = rr")
+
+    # Adam over the network's parameters, then the bf16 repack of the weights
+    net = ws.UNet(seed=0)
+    n_params = sum(w.numel() for w, _, _, _ in net.parameters())
+    n_tensors = len(net.parameters())
+    report("adam", timed(lambda: net.adam(lr=1e-6)), 28.0 * n_params,
+           n_tensors + 2 * len(net.layers),
+           f"{n_params} parameters in {n_tensors} tensors, plus {2 * len(net.layers)} "
+           "k_pack launches (launch-bound)")
+
+    # integer cells of 4M particles in a 1024x1024 fluid
+    spec = wl.PARTICLES_1024
+    from natrix_gb300 import FluidSimulator
+
+    fluid = FluidSimulator(spec.width, spec.height)
+    n = wl.N_PARTICLES
+    parts = LagrangianParticles(fluid, wl.uniform_particles(0, n, spec.width, spec.height))
+    host = torch.empty(n, 2, dtype=torch.int32, pin_memory=True)
+
+    def cells_call():
+        _lib.check(lib.natrix_particles_cells(parts.handle, ctypes.c_void_p(host.data_ptr()), st))
+
+    report("particle_cells", timed(cells_call), 16.0 * n, 1,
+           "k_particle_cells (positions 8 B in, cells 8 B out) plus the 32 MB read-back "
+           "to pinned host memory, which dominates")
+    parts.destroy()
+    fluid.destroy()
+    sim.destroy()
+    worst = min(v["frac"] for k, v in kernels.items() if k not in ("adam", "particle_cells"))
+    print(json.dumps({
+        "metric": "auxiliary kernels: per-region residual HBM GB/s (2048x2048)",
+        "value": kernels["residual_regions"]["gbs"], "unit": "GB/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": kernels["residual_regions"]["us_per_call"] / 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 fields, f64 sums", "data": "synthetic (solver state, seeded fields)",
+        "config": {"workload": "aux-kernels-2048x2048+cg-16x512x512+4M-particles",
+                   "l2": "2048x2048 fields re-read back to back (within L2 between calls)",
+                   "jacobi_variant": variant},
+        "peak": hbm, "peak_kind": kind, "lowest_frac_bandwidth_bound": worst,
+        "kernels": kernels,
+    }), flush=True)
+
+
 def run_unet_forward(args):
     """Warm-start network inference throughput: one forward pass of
     --batch x 512 x 512 (synthetic divergence and obstacle fields) per step,
@@ -843,7 +1023,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["natrix", "reference"], default="natrix")
     ap.add_argument("--workload", choices=["large", "small", "particles", "batch", "warmstart",
-                                           "unet-forward", "unet-train", "render"],
+                                           "unet-forward", "unet-train", "render", "aux"],
                     default="large")
     ap.add_argument("--batch", type=int, default=64, help="unet-forward: images per pass")
     ap.add_argument("--pairs", type=int, default=512, help="warmstart: training pairs")
@@ -868,6 +1048,8 @@ def main():
     if args.workload == "unet-train":
         run_unet_train(args)
         return
+    if args.workload == "aux":
+        return run_aux(args)
     if args.workload == "render":
         run_render(args)
         return

@@ -110,7 +110,8 @@ int natrix_nn_adam(float* w, const float* g, float* m, float* v, int64_t n, floa
  * (dense vectors of H x W per image, mask rows of `pitch` bytes):
  * apply: y = -(A x) on fluid cells (0 on obstacles), A the sweep's operator;
  * dot: out[b] = sum over fluid cells of a*c (out zeroed first);
- * axpy: y += sign * (num[b] / den[b]) * d;  dir: d = r + (rr_new[b] / rr_old[b]) d. */
+ * axpy: y += sign * (num[b] / den[b]) * d;  dir: d = r + (rr_new[b] / rr_old[b]) d.
+ * B up to 65535 and H x W (per) below 2^31, else NATRIX_ERANGE. */
 int natrix_nn_cg_apply(const double* x, const uint8_t* mask, int32_t B, int32_t H, int32_t W,
                        int32_t pitch, double* y, void* stream);
 int natrix_nn_cg_dot(const double* a, const double* c, const uint8_t* mask, int32_t B, int32_t H,

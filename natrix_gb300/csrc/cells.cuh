@@ -304,6 +304,17 @@ __device__ __forceinline__ Nbr nbrs(const Grid& g, int x, int y) {
     return n;
 }
 
+// The same clamped indices from one row offset (no per-neighbour multiply).
+__device__ __forceinline__ Nbr nbrs_at(const Grid& g, int x, int y) {
+    Nbr n;
+    n.c = (size_t)y * g.P + x;
+    n.l = x > 0 ? n.c - 1 : n.c;
+    n.r = x < g.W - 1 ? n.c + 1 : n.c;
+    n.b = y > 0 ? n.c - g.P : n.c;
+    n.t = y < g.H - 1 ? n.c + g.P : n.c;
+    return n;
+}
+
 // ------------------------------------------------------ vorticity confinement
 // shader.CalcVorticity.comp:13-27.
 __device__ __forceinline__ void cell_calc_vorticity(const float2* __restrict__ v, float* __restrict__ w, Grid g, int x, int y) {

@@ -104,6 +104,121 @@ __device__ __forceinline__ float nx_expf(float x) {
 // beyond a wall, where the clamped index of common.sh:9-19 is the cell itself.
 enum : uint8_t { NB_L = 1, NB_R = 2, NB_B = 4, NB_T = 8 };
 
+// ------------------------------------------------------ residual arithmetic
+// The residual of the pressure equation at a fluid cell, r = b - ((x1 + x2 +
+// y1 + y2) - 4 pc) with the sweep's neighbour substitution, and the sums
+// {n, r, r^2, b, b^2} a thread keeps over its cells.
+//
+// GB300 runs FP64 at a small fraction of its FP32 rate, and plain FP32 would
+// lose r to cancellation (near convergence r is tiny next to the pressures),
+// so the arithmetic runs on the FP32 pipe in float-float form (a value is the
+// unevaluated sum hi + lo of two floats):
+//   * r is the compensated sum of the six terms b, -x1, -x2, -y1, -y2, 4 pc
+//     (Ogita, Rump and Oishi's Sum2: a cascade of Knuth's TwoSum with the
+//     rounding errors summed apart), kept as a pair; its error is below
+//     about 1e-13 times the sum of the terms' magnitudes;
+//   * squares are split exactly with a fused multiply-add (TwoProd);
+//   * running sums add pairs with Dekker's add2 (TwoSum of the high parts,
+//     low parts added, then renormalised).
+// Warps sum their threads' pairs the same way; lane 0 converts the warp's
+// pairs to FP64 once, for the block and grid sums.
+struct FF {
+    float h, l;
+};
+
+__device__ __forceinline__ FF two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+
+__device__ __forceinline__ FF two_prod(float a, float b) {
+    const float p = a * b;
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const FF s = two_sum(a.h, b.h);
+    const float e = s.l + (a.l + b.l);
+    const float h = s.h + e;
+    return {h, e - (h - s.h)};
+}
+
+struct ResidSums {
+    int n = 0;
+    FF r{0.0f, 0.0f}, rr{0.0f, 0.0f}, b{0.0f, 0.0f}, bb{0.0f, 0.0f};
+
+    __device__ __forceinline__ void add(float bv, float pc, float x1, float x2, float y1,
+                                        float y2) {
+        FF t = two_sum(bv, -x1);
+        float c = t.l;
+        t = two_sum(t.h, -x2);
+        c += t.l;
+        t = two_sum(t.h, -y1);
+        c += t.l;
+        t = two_sum(t.h, -y2);
+        c += t.l;
+        t = two_sum(t.h, 4.0f * pc);
+        c += t.l;
+        const FF rv = two_sum(t.h, c);
+        n += 1;
+        r = ff_add(r, rv);
+        FF sq = two_prod(rv.h, rv.h);
+        sq.l += 2.0f * rv.h * rv.l;
+        rr = ff_add(rr, sq);
+        b = ff_add(b, FF{bv, 0.0f});
+        bb = ff_add(bb, two_prod(bv, bv));
+    }
+
+    // Sum over the warp into lane 0, in float-float on the FP32 pipe (a
+    // warp sum in FP64 would cost each thread 25 FP64 additions).
+    __device__ __forceinline__ void warp_sum() {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            n += __shfl_down_sync(0xffffffffu, n, o);
+            r = ff_add(r, shfl_down(r, o));
+            rr = ff_add(rr, shfl_down(rr, o));
+            b = ff_add(b, shfl_down(b, o));
+            bb = ff_add(bb, shfl_down(bb, o));
+        }
+    }
+
+    __device__ __forceinline__ static FF shfl_down(FF v, int o) {
+        return {__shfl_down_sync(0xffffffffu, v.h, o), __shfl_down_sync(0xffffffffu, v.l, o)};
+    }
+
+    __device__ __forceinline__ void to_double(double out[5]) const {
+        out[0] = (double)n;
+        out[1] = (double)r.h + (double)r.l;
+        out[2] = (double)rr.h + (double)rr.l;
+        out[3] = (double)b.h + (double)b.l;
+        out[4] = (double)bb.h + (double)bb.l;
+    }
+};
+
+// (x, y) of a linear cell index that advances by a fixed stride: one
+// division when it starts, then an add and a compare per step while rows are
+// at least a stride wide.
+struct CellWalk {
+    int x, y;
+    __device__ __forceinline__ CellWalk(int lin, int W) {
+        y = lin / W;
+        x = lin - y * W;
+    }
+    __device__ __forceinline__ void advance(int stride, int W) {
+        x += stride;
+        if (x >= W) {
+            if (W >= stride) {
+                x -= W;
+                ++y;
+            } else {
+                y += x / W;
+                x %= W;
+            }
+        }
+    }
+};
+
 // Programmatic dependent launch.  The kernels of the single-grid step are
 // launched with programmatic stream serialisation, so a launch is scheduled
 // while its predecessor on the stream drains instead of after it has retired.

@@ -48,51 +48,39 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Same sums and the same block decomposition as the handle-based residual;
-// the neighbour-substitution rule (obstacle neighbour or wall -> centre
-// pressure, shader.Poisson.comp:32-35 with common.sh:9-19 clamping) is
-// evaluated from the mask here instead of precomputed flags.
+// Same sums, arithmetic (natrix::ResidSums) and block decomposition as the
+// handle-based residual; the neighbour-substitution rule (obstacle neighbour
+// or wall -> centre pressure, shader.Poisson.comp:32-35 with common.sh:9-19
+// clamping) is evaluated from the mask here instead of precomputed flags.
 __global__ void __launch_bounds__(kThreads)
     k_residual_noalloc(const float* __restrict__ p, const float* __restrict__ div,
                        const uint8_t* __restrict__ mask, int W, int H, int P,
                        double* __restrict__ partials) {
-    double acc[5] = {0, 0, 0, 0, 0};
-    const long total = (long)W * H;
-    const long base = (long)blockIdx.x * kCellsPerBlock + threadIdx.x;
+    natrix::ResidSums rs;
+    const int total = W * H;  // at most NATRIX_NOALLOC_MAX_CELLS
+    const int base = blockIdx.x * (int)kCellsPerBlock + threadIdx.x;
+    natrix::CellWalk w(base, W);
+#pragma unroll
     for (int k = 0; k < kCellsPerThread; ++k) {
-        const long lin = base + (long)k * kThreads;
-        if (lin >= total) break;
-        const int y = (int)(lin / W), x = (int)(lin % W);
-        const int xl = x > 0 ? x - 1 : 0, xr = x < W - 1 ? x + 1 : W - 1;
-        const int yb = y > 0 ? y - 1 : 0, yt = y < H - 1 ? y + 1 : H - 1;
+        const int lin = base + k * kThreads;
+        const int x = w.x, y = w.y;
+        w.advance(kThreads, W);
+        if (lin >= total) continue;
         const size_t c = (size_t)y * P + x;
-        const size_t l = (size_t)y * P + xl, r = (size_t)y * P + xr;
-        const size_t b = (size_t)yb * P + x, t = (size_t)yt * P + x;
         if (mask && mask[c]) continue;
+        const size_t l = x > 0 ? c - 1 : c, r = x < W - 1 ? c + 1 : c;
+        const size_t b = y > 0 ? c - P : c, t = y < H - 1 ? c + P : c;
         const bool sl = x == 0 || (mask && mask[l]);
         const bool sr = x == W - 1 || (mask && mask[r]);
         const bool sb = y == 0 || (mask && mask[b]);
         const bool st = y == H - 1 || (mask && mask[t]);
-        const double pc = p[c];
-        const double x1 = sl ? pc : (double)p[l];
-        const double x2 = sr ? pc : (double)p[r];
-        const double y1 = sb ? pc : (double)p[b];
-        const double y2 = st ? pc : (double)p[t];
-        const double bb = div[c];
-        const double rr = bb - ((x1 + x2 + y1 + y2) - 4.0 * pc);
-        acc[0] += 1.0;
-        acc[1] += rr;
-        acc[2] += rr * rr;
-        acc[3] += bb;
-        acc[4] += bb * bb;
+        const float pc = p[c];
+        rs.add(div[c], pc, sl ? pc : p[l], sr ? pc : p[r], sb ? pc : p[b], st ? pc : p[t]);
     }
     __shared__ double s_part[kThreads / 32][5];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-        const double v = warp_sum(acc[j]);
-        if (lane == 0) s_part[wid][j] = v;
-    }
+    rs.warp_sum();
+    if (lane == 0) rs.to_double(s_part[wid]);
     __syncthreads();
     if (threadIdx.x < 5) {
         double s = 0;
@@ -101,19 +89,30 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-__global__ void k_residual_noalloc_final(const double* __restrict__ partials, int nblocks,
-                                         double* __restrict__ out) {
-    __shared__ double s[32][5];
-    const int lane = threadIdx.x;
+// One block of 256 threads: each thread sums every 256th block's partials,
+// then the warps and the block reduce (FP64 throughput on one SM bounds this
+// kernel, so few threads: the work is the partials' additions).
+constexpr int kFinalThreads = 256;
+
+__global__ void __launch_bounds__(kFinalThreads)
+    k_residual_noalloc_final(const double* __restrict__ partials, int nblocks,
+                             double* __restrict__ out) {
+    __shared__ double s[kFinalThreads / 32][5];
     double acc[5] = {0, 0, 0, 0, 0};
-    for (int b = lane; b < nblocks; b += 32)
+    for (int b = threadIdx.x; b < nblocks; b += kFinalThreads)
+#pragma unroll
         for (int j = 0; j < 5; ++j) acc[j] += partials[(size_t)b * 5 + j];
-    for (int j = 0; j < 5; ++j) s[lane][j] = acc[j];
-    __syncwarp();
-    if (lane < 5) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        const double v = warp_sum(acc[j]);
+        if (lane == 0) s[wid][j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
         double t = 0;
-        for (int k = 0; k < 32; ++k) t += s[k][lane];
-        out[lane] = t;
+        for (int w = 0; w < kFinalThreads / 32; ++w) t += s[w][threadIdx.x];
+        out[threadIdx.x] = t;
     }
 }
 
@@ -163,7 +162,7 @@ extern "C" int natrix_residual_noalloc(const float* p, const float* div, const u
                                                      partials);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) {
-        k_residual_noalloc_final<<<1, 32, 0, st>>>(partials, nblocks, out_dev);
+        k_residual_noalloc_final<<<1, kFinalThreads, 0, st>>>(partials, nblocks, out_dev);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) return noalloc_fail(NATRIX_ECUDA, cudaGetErrorString(e));

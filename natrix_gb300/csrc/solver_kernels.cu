@@ -535,37 +535,29 @@ __global__ void __launch_bounds__(RES_THREADS)
                const uint8_t* __restrict__ mask, const uint8_t* __restrict__ flags, Grid g,
                const __grid_constant__ StepParams spv, double* __restrict__ partials) {
     const StepParams* sp = &spv;
-    double acc[5] = {0, 0, 0, 0, 0};
-    const long total = (long)g.W * g.H;
-    const long base = (long)blockIdx.x * RES_THREADS * RES_CELLS_PER_THREAD + threadIdx.x;
+    ResidSums rs;
+    const int total = g.W * g.H;  // at most 32768^2 = 2^30 cells
+    const int base = blockIdx.x * RES_THREADS * RES_CELLS_PER_THREAD + threadIdx.x;
     const bool mz = sp->mask_zero != 0;
+    CellWalk w(base, g.W);
+#pragma unroll
     for (int k = 0; k < RES_CELLS_PER_THREAD; ++k) {
-        const long lin = base + (long)k * RES_THREADS;
-        if (lin >= total) break;
-        const int y = (int)(lin / g.W), x = (int)(lin % g.W);
-        const Nbr n = nbrs(g, x, y);
-        if (!mz && mask[n.c]) continue;
-        const uint8_t f = flags[n.c];
-        const double pc = p[n.c];
-        const double x1 = (f & NB_L) ? pc : (double)p[n.l];
-        const double x2 = (f & NB_R) ? pc : (double)p[n.r];
-        const double y1 = (f & NB_B) ? pc : (double)p[n.b];
-        const double y2 = (f & NB_T) ? pc : (double)p[n.t];
-        const double b = div[n.c];
-        const double r = b - ((x1 + x2 + y1 + y2) - 4.0 * pc);
-        acc[0] += 1.0;
-        acc[1] += r;
-        acc[2] += r * r;
-        acc[3] += b;
-        acc[4] += b * b;
+        const int lin = base + k * RES_THREADS;
+        if (lin < total) {
+            const Nbr n = nbrs_at(g, w.x, w.y);
+            if (mz || !mask[n.c]) {
+                const uint8_t f = flags[n.c];
+                const float pc = p[n.c];
+                rs.add(div[n.c], pc, (f & NB_L) ? pc : p[n.l], (f & NB_R) ? pc : p[n.r],
+                       (f & NB_B) ? pc : p[n.b], (f & NB_T) ? pc : p[n.t]);
+            }
+        }
+        w.advance(RES_THREADS, g.W);
     }
     __shared__ double s_part[RES_THREADS / 32][5];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-        const double v = warp_sum(acc[j]);
-        if (lane == 0) s_part[wid][j] = v;
-    }
+    rs.warp_sum();
+    if (lane == 0) rs.to_double(s_part[wid]);
     __syncthreads();
     if (threadIdx.x < 5) {
         double s = 0;
@@ -577,64 +569,103 @@ __global__ void __launch_bounds__(RES_THREADS)
 // The same sums per connected fluid region: labels[y*W + x] in [0, n) for
 // fluid cells, < 0 for obstacle cells.  The pressure system is pure Neumann
 // on each region, so its residual is only defined up to each region's mean.
-// Warps whose lanes share one label (the common case) reduce first and add
-// once; mixed warps add per lane.
+// Each thread takes RES_CELLS_PER_THREAD cells, as k_residual does.
 __global__ void __launch_bounds__(RES_THREADS)
     k_residual_labels(const float* __restrict__ p, const float* __restrict__ div,
                       const uint8_t* __restrict__ flags, const int* __restrict__ labels, Grid g,
                       double* __restrict__ sums) {
-    const long total = (long)g.W * g.H;
-    const long lin = (long)blockIdx.x * RES_THREADS + threadIdx.x;
-    int lab = -1;
-    double v[5] = {0, 0, 0, 0, 0};
-    if (lin < total) {
-        const int y = (int)(lin / g.W), x = (int)(lin % g.W);
-        lab = labels[lin];
+    const int total = g.W * g.H;  // at most 32768^2 = 2^30 cells
+    const int base = blockIdx.x * RES_THREADS * RES_CELLS_PER_THREAD + threadIdx.x;
+    // each thread sums its cells per run of one label and adds a run to the
+    // label's sums when the label changes (only at region boundaries)
+    int cur = -1;
+    ResidSums rs;
+    double v[5];
+    CellWalk w(base, g.W);
+#pragma unroll
+    for (int k = 0; k < RES_CELLS_PER_THREAD; ++k) {
+        const int lin = base + k * RES_THREADS;
+        const int lab = lin < total ? labels[lin] : -1;
         if (lab >= 0) {
-            const Nbr n = nbrs(g, x, y);
+            if (lab != cur) {
+                if (cur >= 0) {
+                    rs.to_double(v);
+#pragma unroll
+                    for (int j = 0; j < 5; ++j) atomicAdd(sums + (size_t)cur * 5 + j, v[j]);
+                    rs = ResidSums();
+                }
+                cur = lab;
+            }
+            const Nbr n = nbrs_at(g, w.x, w.y);
             const uint8_t f = flags[n.c];
-            const double pc = p[n.c];
-            const double x1 = (f & NB_L) ? pc : (double)p[n.l];
-            const double x2 = (f & NB_R) ? pc : (double)p[n.r];
-            const double y1 = (f & NB_B) ? pc : (double)p[n.b];
-            const double y2 = (f & NB_T) ? pc : (double)p[n.t];
-            const double b = div[n.c];
-            const double r = b - ((x1 + x2 + y1 + y2) - 4.0 * pc);
-            v[0] = 1.0;
-            v[1] = r;
-            v[2] = r * r;
-            v[3] = b;
-            v[4] = b * b;
+            const float pc = p[n.c];
+            rs.add(div[n.c], pc, (f & NB_L) ? pc : p[n.l], (f & NB_R) ? pc : p[n.r],
+                   (f & NB_B) ? pc : p[n.b], (f & NB_T) ? pc : p[n.t]);
         }
+        w.advance(RES_THREADS, g.W);
     }
-    const int l0 = __shfl_sync(0xffffffffu, lab, 0);
-    const bool uniform = __all_sync(0xffffffffu, lab == l0);
-    if (uniform) {
-        if (l0 < 0) return;
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-            const double t = warp_sum(v[j]);
-            if ((threadIdx.x & 31) == 0) atomicAdd(sums + (size_t)l0 * 5 + j, t);
+    // a warp whose threads hold one label (or none) sums it with shuffles;
+    // the block then adds each run of consecutive warps with one label as one
+    // atomic per value (the sums are a few addresses every block shares)
+    __shared__ double s_part[RES_THREADS / 32][5];
+    __shared__ int s_lab[RES_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int l0 = __reduce_max_sync(0xffffffffu, cur);
+    if (__all_sync(0xffffffffu, cur == l0 || cur < 0)) {
+        rs.warp_sum();
+        if (lane == 0) {
+            rs.to_double(s_part[wid]);
+            s_lab[wid] = l0;
         }
-    } else if (lab >= 0) {
+    } else {
+        if (cur >= 0) {
+            rs.to_double(v);
 #pragma unroll
-        for (int j = 0; j < 5; ++j) atomicAdd(sums + (size_t)lab * 5 + j, v[j]);
+            for (int j = 0; j < 5; ++j) atomicAdd(sums + (size_t)cur * 5 + j, v[j]);
+        }
+        if (lane == 0) s_lab[wid] = -1;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        int run = -1;
+        double acc = 0.0;
+        for (int w = 0; w < RES_THREADS / 32; ++w) {
+            const int l = s_lab[w];
+            if (l < 0) continue;
+            if (l != run) {
+                if (run >= 0) atomicAdd(sums + (size_t)run * 5 + threadIdx.x, acc);
+                run = l;
+                acc = 0.0;
+            }
+            acc += s_part[w][threadIdx.x];
+        }
+        if (run >= 0) atomicAdd(sums + (size_t)run * 5 + threadIdx.x, acc);
     }
 }
 
-__global__ void k_residual_final(const double* __restrict__ partials, int nblocks,
-                                 double* __restrict__ out) {
-    __shared__ double s[32][5];
-    const int lane = threadIdx.x;  // 32 threads
+// One block of 256 threads: each thread sums every 256th block's partials,
+// then the warps and the block reduce (FP64 throughput on one SM bounds this
+// kernel, so few threads: the work is the partials' additions).
+constexpr int RES_FINAL_THREADS = 256;
+
+__global__ void __launch_bounds__(RES_FINAL_THREADS)
+    k_residual_final(const double* __restrict__ partials, int nblocks, double* __restrict__ out) {
+    __shared__ double s[RES_FINAL_THREADS / 32][5];
     double acc[5] = {0, 0, 0, 0, 0};
-    for (int b = lane; b < nblocks; b += 32)
+    for (int b = threadIdx.x; b < nblocks; b += RES_FINAL_THREADS)
+#pragma unroll
         for (int j = 0; j < 5; ++j) acc[j] += partials[(size_t)b * 5 + j];
-    for (int j = 0; j < 5; ++j) s[lane][j] = acc[j];
-    __syncwarp();
-    if (lane < 5) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        const double v = warp_sum(acc[j]);
+        if (lane == 0) s[wid][j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
         double t = 0;
-        for (int k = 0; k < 32; ++k) t += s[k][lane];
-        out[lane] = t;
+        for (int w = 0; w < RES_FINAL_THREADS / 32; ++w) t += s[w][threadIdx.x];
+        out[threadIdx.x] = t;
     }
 }
 
@@ -646,7 +677,8 @@ cudaError_t launch_residual_labels(const float* p, const float* div, const uint8
     cudaError_t e = cudaMemsetAsync(sums, 0, (size_t)n_labels * 5 * sizeof(double), st);
     if (e != cudaSuccess) return e;
     const long total = (long)g.W * g.H;
-    k_residual_labels<<<(unsigned)((total + RES_THREADS - 1) / RES_THREADS), RES_THREADS, 0, st>>>(
+    const long per_block = (long)RES_THREADS * RES_CELLS_PER_THREAD;
+    k_residual_labels<<<(unsigned)((total + per_block - 1) / per_block), RES_THREADS, 0, st>>>(
         p, div, flags, labels, g, sums);
     return cudaGetLastError();
 }
@@ -851,7 +883,7 @@ cudaError_t launch_residual(const float* p, const float* div, const uint8_t* mas
     k_residual<<<nb, RES_THREADS, 0, st>>>(p, div, mask, flags, g, sp, partials);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_residual_final<<<1, 32, 0, st>>>(partials, nb, out);
+    k_residual_final<<<1, RES_FINAL_THREADS, 0, st>>>(partials, nb, out);
     return cudaGetLastError();
 }
 

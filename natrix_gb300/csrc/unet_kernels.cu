@@ -511,41 +511,48 @@ __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float
 }
 
 // ---------------------------------------------------------- FP64 CG solver
-// Dense per-image vectors (stride H*W); mask pitch P (bytes per row).
-__global__ void k_cg_apply(const double* __restrict__ x, const uint8_t* __restrict__ mask, int B,
-                           int H, int W, int P, double* __restrict__ y) {
-    const long n = (long)B * H * W;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-         i += (long)gridDim.x * blockDim.x) {
-        const int b = (int)(i / ((long)H * W));
-        const long k = i % ((long)H * W);
-        const int xx = (int)(k % W), yy = (int)(k / W);
-        const size_t mb = (size_t)b * H * P;
-        if (mask && mask[mb + (size_t)yy * P + xx]) {
-            y[i] = 0.0;
-            continue;
+// Dense per-image vectors (stride H*W); mask pitch P (bytes per row).  The
+// kernels run on a per-image grid (blockIdx.y = image) with 32-bit indices
+// inside an image (H*W < 2^31), and read per-image scalars once per block.
+__global__ void __launch_bounds__(256)
+    k_cg_apply(const double* __restrict__ x, const uint8_t* __restrict__ mask, int H, int W,
+               int P, double* __restrict__ y) {
+    const int b = blockIdx.y;
+    const size_t base = (size_t)b * H * W, mb = (size_t)b * H * P;
+    for (int yy = blockIdx.x; yy < H; yy += gridDim.x) {
+        const double* xr = x + base + (size_t)yy * W;
+        double* yr = y + base + (size_t)yy * W;
+        const uint8_t* mr = mask ? mask + mb + (size_t)yy * P : nullptr;
+        for (int xx = threadIdx.x; xx < W; xx += blockDim.x) {
+            if (mr && mr[xx]) {
+                yr[xx] = 0.0;
+                continue;
+            }
+            bool sl, sr, sb, st;
+            nbr_sub(mask, xx, yy, W, H, P, mb, sl, sr, sb, st);
+            // substituted neighbours read the centre itself (indices stay in the image)
+            const double c = xr[xx];
+            const double l = xr[sl ? xx : xx - 1], r = xr[sr ? xx : xx + 1];
+            const double bo = xr[sb ? xx : xx - W], t = xr[st ? xx : xx + W];
+            // negated so the operator is positive semi-definite for CG
+            yr[xx] = -((((l + r) + bo) + t) - 4.0 * c);
         }
-        bool sl, sr, sb, st;
-        nbr_sub(mask, xx, yy, W, H, P, mb, sl, sr, sb, st);
-        const double c = x[i];
-        const double l = sl ? c : x[i - 1], r = sr ? c : x[i + 1];
-        const double bo = sb ? c : x[i - W], t = st ? c : x[i + W];
-        // negated so the operator is positive semi-definite for CG
-        y[i] = -((((l + r) + bo) + t) - 4.0 * c);
     }
 }
 
-// out[b] += sum over image b of a*b (fluid cells only when mask given)
+// out[b] += sum over image b of a*c (fluid cells only when mask given)
 __global__ void __launch_bounds__(256)
     k_cg_dot(const double* __restrict__ a, const double* __restrict__ c,
              const uint8_t* __restrict__ mask, int H, int W, int P, double* __restrict__ out) {
     const int b = blockIdx.y;
     const size_t base = (size_t)b * H * W, mb = (size_t)b * H * P;
     double acc = 0;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < (long)H * W;
-         i += (long)gridDim.x * blockDim.x) {
-        if (mask && mask[mb + (i / W) * P + i % W]) continue;
-        acc += a[base + i] * c[base + i];
+    for (int yy = blockIdx.x; yy < H; yy += gridDim.x) {
+        const double* ar = a + base + (size_t)yy * W;
+        const double* cr = c + base + (size_t)yy * W;
+        const uint8_t* mr = mask ? mask + mb + (size_t)yy * P : nullptr;
+        for (int xx = threadIdx.x; xx < W; xx += blockDim.x)
+            if (!mr || !mr[xx]) acc += ar[xx] * cr[xx];
     }
     acc = warp_sum_d(acc);
     __shared__ double s[8];
@@ -558,30 +565,97 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// y = x + alpha[b] * y_scale * d   (per image coefficient; sign selects +/-)
-__global__ void k_cg_axpy(double* __restrict__ y, const double* __restrict__ d,
-                          const double* __restrict__ num, const double* __restrict__ den,
-                          double sign, int B, long per) {
-    const long n = (long)B * per;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-         i += (long)gridDim.x * blockDim.x) {
-        const int b = (int)(i / per);
-        const double a = den[b] != 0.0 ? num[b] / den[b] : 0.0;
-        y[i] += sign * a * d[i];
+// y += sign * (num[b] / den[b]) * d, two elements per thread and iteration
+// when `vec` (cg_vec: even image stride, 16-byte aligned vectors)
+__global__ void __launch_bounds__(256)
+    k_cg_axpy(double* __restrict__ y, const double* __restrict__ d,
+              const double* __restrict__ num, const double* __restrict__ den, double sign,
+              int per, bool vec) {
+    const int b = blockIdx.y;
+    __shared__ double s_a;
+    if (threadIdx.x == 0) s_a = den[b] != 0.0 ? sign * (num[b] / den[b]) : 0.0;
+    __syncthreads();
+    const double a = s_a;
+    const size_t base = (size_t)b * per;
+    const int stride = gridDim.x * blockDim.x;
+    if (vec) {
+        double2* y2 = reinterpret_cast<double2*>(y + base);
+        const double2* d2 = reinterpret_cast<const double2*>(d + base);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < per / 2; i += stride) {
+            double2 v = y2[i];
+            const double2 w = d2[i];
+            v.x += a * w.x;
+            v.y += a * w.y;
+            y2[i] = v;
+        }
+    } else {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < per; i += stride)
+            y[base + i] += a * d[base + i];
     }
 }
 
-// d = r + (rr_new / rr_old) d
-__global__ void k_cg_dir(double* __restrict__ d, const double* __restrict__ r,
-                         const double* __restrict__ rr_new, const double* __restrict__ rr_old,
-                         int B, long per) {
-    const long n = (long)B * per;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-         i += (long)gridDim.x * blockDim.x) {
-        const int b = (int)(i / per);
-        const double beta = rr_old[b] != 0.0 ? rr_new[b] / rr_old[b] : 0.0;
-        d[i] = r[i] + beta * d[i];
+// d = r + (rr_new[b] / rr_old[b]) d, two elements at a time when `vec`
+__global__ void __launch_bounds__(256)
+    k_cg_dir(double* __restrict__ d, const double* __restrict__ r,
+             const double* __restrict__ rr_new, const double* __restrict__ rr_old, int per,
+             bool vec) {
+    const int b = blockIdx.y;
+    __shared__ double s_beta;
+    if (threadIdx.x == 0) s_beta = rr_old[b] != 0.0 ? rr_new[b] / rr_old[b] : 0.0;
+    __syncthreads();
+    const double beta = s_beta;
+    const size_t base = (size_t)b * per;
+    const int stride = gridDim.x * blockDim.x;
+    if (vec) {
+        double2* d2 = reinterpret_cast<double2*>(d + base);
+        const double2* r2 = reinterpret_cast<const double2*>(r + base);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < per / 2; i += stride) {
+            double2 v = d2[i];
+            const double2 w = r2[i];
+            v.x = w.x + beta * v.x;
+            v.y = w.y + beta * v.y;
+            d2[i] = v;
+        }
+    } else {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < per; i += stride)
+            d[base + i] = r[base + i] + beta * d[base + i];
     }
+}
+
+// Blocks per image for the CG kernels: about eight blocks of 256 threads per
+// SM over the whole batch (full occupancy), at most one thread per element
+// (or element pair).
+unsigned cg_blocks(long work_per_image, int B) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            sms < 1)
+            sms = 1;
+    }
+    const long per_image = (8L * sms + B - 1) / B;
+    const long need = blocks(work_per_image, 256);
+    return (unsigned)(need < per_image ? need : per_image);
+}
+
+// Blocks per image for the row loops of apply and dot: at most one per row.
+unsigned cg_rows(int H, int B) {
+    const unsigned n = cg_blocks(1L << 30, B);
+    return n < (unsigned)H ? n : (unsigned)H;
+}
+
+// Whether two-element (16-byte) accesses are valid: even image stride and
+// 16-byte aligned vectors.
+bool cg_vec(long per, const void* a, const void* b) {
+    return (per & 1) == 0 && (((uintptr_t)a | (uintptr_t)b) & 15) == 0;
+}
+
+// The per-image grid holds up to 65535 images; indices inside an image are 32-bit.
+int cg_range(long B, long per) {
+    if (B > 65535 || per >= (1L << 31))
+        return set_last_error(NATRIX_ERANGE, "CG: more than 65535 images or 2^31 cells per image");
+    return NATRIX_OK;
 }
 
 }  // namespace
@@ -709,38 +783,42 @@ int natrix_nn_adam(float* w, const float* g, float* m, float* v, int64_t n, floa
 int natrix_nn_cg_apply(const double* x, const uint8_t* mask, int32_t B, int32_t H, int32_t W,
                        int32_t P, double* y, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const long n = (long)B * H * W;
-    k_cg_apply<<<blocks(n, 256) < 16384 ? blocks(n, 256) : 16384, 256, 0, st>>>(x, mask, B, H, W,
-                                                                                P, y);
+    if (B < 1) return NATRIX_OK;
+    if (int rc = cg_range(B, (long)H * W)) return rc;
+    k_cg_apply<<<dim3(cg_rows(H, B), B), 256, 0, st>>>(x, mask, H, W, P, y);
     return launch_status();
 }
 
 int natrix_nn_cg_dot(const double* a, const double* c, const uint8_t* mask, int32_t B, int32_t H,
                      int32_t W, int32_t P, double* out, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (B < 1) return NATRIX_OK;
+    if (int rc = cg_range(B, (long)H * W)) return rc;
     if (cudaMemsetAsync(out, 0, (size_t)B * sizeof(double), st) != cudaSuccess)
         return launch_status();
-    const long per = (long)H * W;
-    const unsigned bx = blocks(per, 256) < 128 ? blocks(per, 256) : 128;
-    k_cg_dot<<<dim3(bx, B), 256, 0, st>>>(a, c, mask, H, W, P, out);
+    k_cg_dot<<<dim3(cg_rows(H, B), B), 256, 0, st>>>(a, c, mask, H, W, P, out);
     return launch_status();
 }
 
 int natrix_nn_cg_axpy(double* y, const double* d, const double* num, const double* den,
                       double sign, int32_t B, int64_t per, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const long n = (long)B * per;
-    k_cg_axpy<<<blocks(n, 256) < 16384 ? blocks(n, 256) : 16384, 256, 0, st>>>(y, d, num, den, sign,
-                                                                               B, per);
+    if (B < 1 || per < 1) return NATRIX_OK;
+    if (int rc = cg_range(B, per)) return rc;
+    const bool vec = cg_vec(per, y, d);
+    k_cg_axpy<<<dim3(cg_blocks(vec ? per / 2 : per, B), B), 256, 0, st>>>(y, d, num, den, sign,
+                                                                           (int)per, vec);
     return launch_status();
 }
 
 int natrix_nn_cg_dir(double* d, const double* r, const double* rr_new, const double* rr_old,
                      int32_t B, int64_t per, void* stream) {
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const long n = (long)B * per;
-    k_cg_dir<<<blocks(n, 256) < 16384 ? blocks(n, 256) : 16384, 256, 0, st>>>(d, r, rr_new, rr_old,
-                                                                              B, per);
+    if (B < 1 || per < 1) return NATRIX_OK;
+    if (int rc = cg_range(B, per)) return rc;
+    const bool vec = cg_vec(per, d, r);
+    k_cg_dir<<<dim3(cg_blocks(vec ? per / 2 : per, B), B), 256, 0, st>>>(d, r, rr_new, rr_old,
+                                                                          (int)per, vec);
     return launch_status();
 }
 

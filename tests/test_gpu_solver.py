@@ -257,6 +257,40 @@ def test_jacobi_sweeps_isolated(cuda, oracle):
     sim.destroy()
 
 
+def test_residual_regions_many_pockets(cuda, oracle):
+    """Per-region residual sums on an obstacle lattice that cuts the grid into
+    hundreds of small pockets: threads, warps and blocks span many labels, so
+    the per-run, per-warp and per-block merging all run."""
+    import torch
+
+    from natrix_gb300 import _lib
+
+    W, H = 301, 203
+    sim, den, ref, rden = make_pair(oracle, W, H, iterations=1, speed=5.0)
+    mask = np.zeros((H, W), np.uint8)
+    mask[:, ::7] = 1
+    mask[::5, :] = 1
+    mask[5::10, 3::14] = 0  # gaps in some walls join pairs of pockets
+    sim.upload(_lib.FIELD_OBSTACLES, mask)
+    sim.update(1 / 60)
+    rng = np.random.default_rng(13)
+    p = rng.normal(size=(H, W)).astype(np.float32)
+    b = rng.normal(size=(H, W)).astype(np.float32)
+    sim.upload(_lib.FIELD_PRESSURE, p)
+    sim.upload(_lib.FIELD_DIVERGENCE, b)
+    labels, n = oracle.fluid_labels(mask)
+    assert n > 500
+    want = oracle.residual_sums_regions(p, b, mask, labels, n)
+    got = torch.empty(n, 5, dtype=torch.float64, device="cuda")
+    _lib.call("natrix_residual_regions", sim.handle,
+              ctypes.c_void_p(torch.from_numpy(labels).cuda().data_ptr()), n,
+              ctypes.c_void_p(got.data_ptr()), None)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(got.cpu().numpy(), want, rtol=1e-9, atol=1e-9)
+    den.destroy()
+    sim.destroy()
+
+
 def test_float64_tolerance(cuda, oracle):
     """GPU float32 vs the float64 oracle after 1 and 10 steps, within the
     stated tolerance (tests/tolerances.py)."""

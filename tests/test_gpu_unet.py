@@ -251,6 +251,77 @@ def test_adam_matches_formula(cuda):
     close(w, wr, rtol=1e-6, what="adam")
 
 
+@pytest.mark.parametrize("B,H,W", [(3, 40, 52), (2, 7, 9)])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_cg_kernels_match_numpy(cuda, B, H, W, offset):
+    """The FP64 conjugate-gradient building blocks against NumPy on the same
+    inputs: the negated sweep operator (obstacle neighbours and walls replaced
+    by the centre, 0 on obstacles), per-image dots over fluid cells, axpy and
+    direction updates; even and odd image sizes, and vectors that start one
+    element past a 16-byte boundary (offset 1: the element-wise path)."""
+    import torch
+
+    from natrix_gb300.core import warmstart as ws
+
+    P = (W + 31) // 32 * 32
+    per = H * W
+    rng = np.random.default_rng(B * 1000 + H * W + offset)
+    mask = (rng.random((B, H, P)) < 0.15).astype(np.uint8)
+    fluid = mask[:, :, :W] == 0
+
+    def dev(a):
+        buf = torch.zeros(a.size + offset, dtype=torch.float64, device="cuda")
+        v = buf[offset:]
+        v.copy_(torch.from_numpy(np.ascontiguousarray(a, np.float64)).view(-1))
+        return v
+
+    def apply_np(x):
+        y = np.zeros_like(x)
+        for b in range(B):
+            m = mask[b, :, :W]
+            for yy in range(H):
+                for xx in range(W):
+                    if m[yy, xx]:
+                        continue
+                    c = x[b, yy, xx]
+                    l = c if xx == 0 or m[yy, xx - 1] else x[b, yy, xx - 1]
+                    r = c if xx == W - 1 or m[yy, xx + 1] else x[b, yy, xx + 1]
+                    bo = c if yy == 0 or m[yy - 1, xx] else x[b, yy - 1, xx]
+                    t = c if yy == H - 1 or m[yy + 1, xx] else x[b, yy + 1, xx]
+                    y[b, yy, xx] = -((((l + r) + bo) + t) - 4.0 * c)
+        return y
+
+    x = rng.normal(size=(B, H, W))
+    d = rng.normal(size=(B, H, W))
+    r = rng.normal(size=(B, H, W))
+    num, den = rng.normal(size=B), rng.normal(size=B)
+    den[0] = 0.0  # a zero denominator gives a zero coefficient
+    dm = torch.from_numpy(mask).cuda()
+    xd, yd = dev(x), dev(np.zeros_like(x))
+    ws._call("natrix_nn_cg_apply", ws._p(xd), ws._p(dm), B, H, W, P, ws._p(yd), ws._s())
+    out = torch.empty(B, dtype=torch.float64, device="cuda")
+    dd = dev(d)
+    ws._call("natrix_nn_cg_dot", ws._p(xd), ws._p(dd), ws._p(dm), B, H, W, P, ws._p(out),
+             ws._s())
+    numd, dend = torch.from_numpy(num).cuda(), torch.from_numpy(den).cuda()
+    ax = dev(x)
+    ws._call("natrix_nn_cg_axpy", ws._p(ax), ws._p(dd), ws._p(numd), ws._p(dend), -1.0, B, per,
+             ws._s())
+    dir_d, rd = dev(d), dev(r)
+    ws._call("natrix_nn_cg_dir", ws._p(dir_d), ws._p(rd), ws._p(numd), ws._p(dend), B, per,
+             ws._s())
+    torch.cuda.synchronize()
+    coef = np.where(den != 0.0, num / np.where(den != 0.0, den, 1.0), 0.0).reshape(B, 1, 1)
+    np.testing.assert_allclose(yd.cpu().numpy().reshape(B, H, W), apply_np(x), rtol=1e-14,
+                               atol=1e-13)
+    np.testing.assert_allclose(out.cpu().numpy(), (x * d * fluid).sum(axis=(1, 2)), rtol=1e-12,
+                               atol=1e-12)
+    np.testing.assert_allclose(ax.cpu().numpy().reshape(B, H, W), x - coef * d, rtol=1e-14,
+                               atol=1e-14)
+    np.testing.assert_allclose(dir_d.cpu().numpy().reshape(B, H, W), r + coef * d, rtol=1e-14,
+                               atol=1e-14)
+
+
 def test_cg_targets_reach_tolerance(cuda, oracle):
     import torch
 
