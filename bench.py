@@ -387,7 +387,14 @@ def run_natrix(args, spec):
                 "bytes_per_cell_step": step_b,
                 "achieved_gbs": value * step_b / 1e9,
                 "frac": value * step_b / 1e9 / peak,
-                "peak_gbs": peak, "peak_kind": peak_kind},
+                "peak_gbs": peak, "peak_kind": peak_kind,
+                "frac_of_nominal_8000": value * step_b / 1e9 / 8000.0},
+            # Jacobi cell-sweeps per second: inside the step (all K sweeps of
+            # every timed step over the whole step time) and inside the
+            # Jacobi phase alone (sweeps over the phase's own launch time)
+            "jacobi_cell_sweeps_per_s": {
+                "per_step_time": value * spec.iterations,
+                "per_jacobi_time": cells * sweeps_per_launch / (launch_ms / 1e3) * world},
             "roofline": {"kernel": "jacobi (temporally blocked, TMA tiles)", "bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
