@@ -142,6 +142,13 @@ int natrix_jacobi(natrix_sim* sim, int32_t sweeps, void* stream);
  * an error status (bounded waits that ran out).  Clears the status. */
 int natrix_sync(natrix_sim* sim, void* stream);
 
+/* Fault injection on the host side, for tests of the error path: write
+ * `status` into the handle's device status word on `stream`, as a kernel
+ * whose bounded wait ran out does (status bit 1: a sweep's tile wait).  The
+ * next natrix_sync returns NATRIX_EDEVICE and clears the word.  Nothing stalls
+ * or faults on the GPU.  No reference counterpart. */
+int natrix_inject_status(natrix_sim* sim, int32_t status, void* stream);
+
 /* --- density grid: SmoothParticlesArea (demo/smooth_particles_area.py) --- */
 
 /* Density grid of its own size, advected by `fluid`'s velocity

@@ -75,6 +75,7 @@ SIGNATURES = {
     "natrix_jacobi": [_vp, _i, _vp],
     "natrix_residual_regions": [_vp, _vp, _i, _vp, _vp],
     "natrix_sync": [_vp, _vp],
+    "natrix_inject_status": [_vp, _i, _vp],
     "natrix_set_timing": [_vp, _i],
     "natrix_get_stats": [_vp, ctypes.POINTER(Stats), _i],
     "natrix_density_create": [_vp, _i, _i, _vpp],

@@ -646,6 +646,16 @@ int natrix_sync(natrix_sim* s, void* stream) {
     return NATRIX_OK;
 }
 
+int natrix_inject_status(natrix_sim* s, int32_t status, void* stream) {
+    if (!s) return fail(NATRIX_EINVAL, "NULL handle");
+    DeviceGuard dg(s->device);
+    cudaStream_t st = stream_of(s, stream);
+    // from pageable memory: the call returns once the value is staged
+    const int v = status;
+    NX_CUDA(cudaMemcpyAsync(s->d_status, &v, sizeof(int), cudaMemcpyHostToDevice, st));
+    return NATRIX_OK;
+}
+
 int natrix_set_timing(natrix_sim* s, int32_t enable) {
     if (!s) return fail(NATRIX_EINVAL, "NULL handle");
     s->timing = enable != 0;

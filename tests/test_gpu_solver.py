@@ -291,6 +291,77 @@ def test_residual_regions_many_pockets(cuda, oracle):
     sim.destroy()
 
 
+def test_device_status_reported_and_cleared(cuda, oracle):
+    """The error path of the kernels' bounded waits, driven from the host: a
+    status word written as a sweep whose tile wait ran out would write it
+    makes natrix_sync fail once with NATRIX_EDEVICE, the next sync is clean,
+    and the handle keeps stepping bit-exact with the oracle (the context stays
+    usable).  Nothing stalls or faults on the GPU."""
+    from natrix_gb300 import _lib
+
+    W, H = 96, 64
+    sim, den, ref, rden = make_pair(oracle, W, H, iterations=10, vorticity=0.2, speed=5.0,
+                                    dissipation=0.99)
+    run_workload(sim, den, ref, rden, steps=2, n_splats=3, n_obst=2, seed=3)
+    sim.sync()
+    _lib.call("natrix_inject_status", sim.handle, 1, None)
+    with pytest.raises(_lib.NatrixError) as err:
+        sim.sync()
+    assert err.value.code == _lib.NATRIX_EDEVICE and "0x1" in str(err.value)
+    sim.sync()  # the status was cleared
+    run_workload(sim, den, ref, rden, steps=2, n_splats=3, n_obst=2, seed=4)
+    got, want = fields(sim, den), ref_fields(ref, rden)
+    for k, v in got.items():
+        assert_equal_f32(v, want[k], f"{k} after the reported status")
+    den.destroy()
+    sim.destroy()
+
+
+def test_non_finite_inputs_match_oracle(cuda, oracle):
+    """NaN and infinite velocities and densities (a caller's upload) go through
+    the same rules as in the oracle: clamp(NaN) gives the lower bound, a NaN
+    sample position clamps to index 0, infinities saturate to the edge; finite
+    results are equal bit for bit and NaNs sit in the same cells."""
+    from natrix_gb300 import _lib
+
+    W, H = 64, 48
+    sim, den, ref, rden = make_pair(oracle, W, H, iterations=12, vorticity=0.3, viscosity=0.1,
+                                    speed=5.0, dissipation=0.99)
+    rng = np.random.default_rng(17)
+    v = rng.uniform(-1, 1, (H, W, 2)).astype(np.float32)
+    v[5, 7, 0] = np.nan
+    v[10, 20, 1] = np.inf
+    v[30, 40, :] = -np.inf
+    v[0, 0, :] = np.nan
+    v[47, 63, 0] = np.inf
+    rho = rng.uniform(0, 1, (H, W)).astype(np.float32)
+    rho[20, 30] = np.nan
+    rho[21, 31] = np.inf
+    sim.upload(_lib.FIELD_VELOCITY, v)
+    ref.velocity[...] = v
+    den.upload(rho)
+    rden.field[...] = rho
+
+    def same(got, want, what):
+        got, want = np.asarray(got), np.asarray(want)
+        gn, wn = np.isnan(got), np.isnan(want)
+        assert np.array_equal(gn, wn), f"{what}: NaN cells differ ({gn.sum()} vs {wn.sum()})"
+        assert np.array_equal(got[~gn], want[~wn]), f"{what}: finite values differ"
+
+    for step in range(3):
+        for s in (sim, ref):
+            s.add_circle_obstacle((0.3, 0.6), 4.0)
+        sim.update(1 / 60)
+        den.update(1 / 60)
+        ref.update(1 / 60)
+        rden.update(1 / 60)
+        got, want = fields(sim, den), ref_fields(ref, rden)
+        for k, val in got.items():
+            same(val, want[k], f"{k} step {step}")
+    den.destroy()
+    sim.destroy()
+
+
 def test_float64_tolerance(cuda, oracle):
     """GPU float32 vs the float64 oracle after 1 and 10 steps, within the
     stated tolerance (tests/tolerances.py)."""
