@@ -816,7 +816,8 @@ def run_aux(args):
     written once): residual 10 (pressure, divergence, mask, flags), per-region
     residual 13 (pressure, divergence, flags, label), allocation-free 9
     (pressure, divergence, mask), sweep launch 13, CG apply 17 (direction 8,
-    mask 1, product 8), dot 17, axpy 24, direction update 24, Adam 28 per
+    mask 1, product 8), dot 17, axpy 24, direction update 24, fused apply+dot
+    17, fused update 48 (x, r, d, q read; x, r written), Adam 28 per
     parameter (weight, gradient, two moments read; weight and moments
     written)."""
     import torch
@@ -930,6 +931,14 @@ def run_aux(args):
     report("cg_dir", timed(lambda: ws._call("natrix_nn_cg_dir", P_(d), P_(r), P_(rr2), P_(rr), B,
                                             per, S())), 24.0 * n_el, 1,
            "direction = r + (rr_new / rr) direction, with rr_new = rr")
+    report("cg_apply_dot", timed(lambda: ws._call("natrix_nn_cg_apply_dot", P_(d), P_(m), B, H, W,
+                                                  P, P_(q), P_(dq), S())), 17.0 * n_el, 1,
+           "fused apply and d.q (q = 0 on obstacles)")
+    # update with rr = 0: x and r are rewritten unchanged, rr_new recomputed
+    zero = torch.zeros_like(rr)
+    report("cg_update", timed(lambda: ws._call("natrix_nn_cg_update", P_(x), P_(r), P_(d), P_(q),
+                                               P_(zero), P_(dq), P_(rr2), B, per, S())),
+           48.0 * n_el, 1, "fused x += a d, r -= a q and r.r")
 
     # Adam over the network's parameters, then the bf16 repack of the weights
     net = ws.UNet(seed=0)

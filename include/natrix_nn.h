@@ -120,6 +120,16 @@ int natrix_nn_cg_axpy(double* y, const double* d, const double* num, const doubl
                       double sign, int32_t B, int64_t per, void* stream);
 int natrix_nn_cg_dir(double* d, const double* r, const double* rr_new, const double* rr_old,
                      int32_t B, int64_t per, void* stream);
+/* Fused steps of one CG iteration (the same arithmetic as the calls they
+ * replace, fewer passes over memory):
+ * apply_dot: q = -(A d) as natrix_nn_cg_apply, and dq[b] = d . q (dq zeroed
+ * first; q is 0 on obstacle cells);
+ * update: with alpha = rr[b] / dq[b] (0 when dq[b] is 0), x += alpha d,
+ * r -= alpha q, and rr_new[b] = r . r (zeroed first).  Same limits. */
+int natrix_nn_cg_apply_dot(const double* d, const uint8_t* mask, int32_t B, int32_t H, int32_t W,
+                           int32_t pitch, double* q, double* dq, void* stream);
+int natrix_nn_cg_update(double* x, double* r, const double* d, const double* q, const double* rr,
+                        const double* dq, double* rr_new, int32_t B, int64_t per, void* stream);
 
 #ifdef __cplusplus
 }

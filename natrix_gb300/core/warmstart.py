@@ -65,6 +65,8 @@ _SIGS = {
     "natrix_nn_cg_dot": [_P, _P, _P, _I, _I, _I, _I, _P, _P],
     "natrix_nn_cg_axpy": [_P, _P, _P, _P, _D, _I, _I64, _P],
     "natrix_nn_cg_dir": [_P, _P, _P, _P, _I, _I64, _P],
+    "natrix_nn_cg_apply_dot": [_P, _P, _I, _I, _I, _I, _P, _P, _P],
+    "natrix_nn_cg_update": [_P, _P, _P, _P, _P, _P, _P, _I, _I64, _P],
 }
 _bound = False
 
@@ -484,11 +486,10 @@ def cg_solve(div: torch.Tensor, mask: Optional[torch.Tensor], inv_scale: torch.T
     it = 0
     rel = torch.ones(B, dtype=torch.float64)
     while it < max_iter:
-        _call("natrix_nn_cg_apply", _p(d), mp, B, H, W, pitch, _p(q), _s())
-        _call("natrix_nn_cg_dot", _p(d), _p(q), mp, B, H, W, pitch, _p(dq), _s())
-        _call("natrix_nn_cg_axpy", _p(x), _p(d), _p(rr), _p(dq), 1.0, B, per, _s())
-        _call("natrix_nn_cg_axpy", _p(r), _p(q), _p(rr), _p(dq), -1.0, B, per, _s())
-        _call("natrix_nn_cg_dot", _p(r), _p(r), mp, B, H, W, pitch, _p(rr_new), _s())
+        # q = -A d and d.q; x += a d, r -= a q and r.r (a = rr / d.q); d = r + b d
+        _call("natrix_nn_cg_apply_dot", _p(d), mp, B, H, W, pitch, _p(q), _p(dq), _s())
+        _call("natrix_nn_cg_update", _p(x), _p(r), _p(d), _p(q), _p(rr), _p(dq), _p(rr_new), B,
+              per, _s())
         _call("natrix_nn_cg_dir", _p(d), _p(r), _p(rr_new), _p(rr), B, per, _s())
         rr, rr_new = rr_new, rr
         it += 1

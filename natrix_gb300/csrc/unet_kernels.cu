@@ -622,6 +622,92 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Block sum of one double per thread, added to out[b] by thread 0.
+__device__ __forceinline__ void block_add_d(double v, double* out) {
+    v = warp_sum_d(v);
+    __shared__ double s[8];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int k = 0; k < 8; ++k) t += s[k];
+        atomicAdd(out, t);
+    }
+}
+
+// q = -(A d) as k_cg_apply, and dq[b] += d . q over the image (q is 0 on
+// obstacle cells, so the sum is over fluid cells): one pass instead of
+// apply + dot.
+__global__ void __launch_bounds__(256)
+    k_cg_apply_dot(const double* __restrict__ d, const uint8_t* __restrict__ mask, int H, int W,
+                   int P, double* __restrict__ q, double* __restrict__ dq) {
+    const int b = blockIdx.y;
+    const size_t base = (size_t)b * H * W, mb = (size_t)b * H * P;
+    double acc = 0.0;
+    for (int yy = blockIdx.x; yy < H; yy += gridDim.x) {
+        const double* xr = d + base + (size_t)yy * W;
+        double* yr = q + base + (size_t)yy * W;
+        const uint8_t* mr = mask ? mask + mb + (size_t)yy * P : nullptr;
+        for (int xx = threadIdx.x; xx < W; xx += blockDim.x) {
+            if (mr && mr[xx]) {
+                yr[xx] = 0.0;
+                continue;
+            }
+            bool sl, sr, sb, st;
+            nbr_sub(mask, xx, yy, W, H, P, mb, sl, sr, sb, st);
+            const double c = xr[xx];
+            const double l = xr[sl ? xx : xx - 1], r = xr[sr ? xx : xx + 1];
+            const double bo = xr[sb ? xx : xx - W], t = xr[st ? xx : xx + W];
+            const double v = -((((l + r) + bo) + t) - 4.0 * c);
+            yr[xx] = v;
+            acc += c * v;
+        }
+    }
+    block_add_d(acc, dq + b);
+}
+
+// With alpha = rr[b] / dq[b]: x += alpha d, r -= alpha q, and rr_new[b] +=
+// r . r (r is 0 on obstacle cells): the two axpys and the next dot in one
+// pass.
+__global__ void __launch_bounds__(256)
+    k_cg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ d,
+                const double* __restrict__ q, const double* __restrict__ rr,
+                const double* __restrict__ dq, double* __restrict__ rr_new, int per, bool vec) {
+    const int b = blockIdx.y;
+    __shared__ double s_a;
+    if (threadIdx.x == 0) s_a = dq[b] != 0.0 ? rr[b] / dq[b] : 0.0;
+    __syncthreads();
+    const double a = s_a;
+    const size_t base = (size_t)b * per;
+    const int stride = gridDim.x * blockDim.x;
+    double acc = 0.0;
+    if (vec) {
+        double2* x2 = reinterpret_cast<double2*>(x + base);
+        double2* r2 = reinterpret_cast<double2*>(r + base);
+        const double2* d2 = reinterpret_cast<const double2*>(d + base);
+        const double2* q2 = reinterpret_cast<const double2*>(q + base);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < per / 2; i += stride) {
+            double2 xv = x2[i], rv = r2[i];
+            const double2 dv = d2[i], qv = q2[i];
+            xv.x += a * dv.x;
+            xv.y += a * dv.y;
+            rv.x -= a * qv.x;
+            rv.y -= a * qv.y;
+            x2[i] = xv;
+            r2[i] = rv;
+            acc += rv.x * rv.x + rv.y * rv.y;
+        }
+    } else {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < per; i += stride) {
+            x[base + i] += a * d[base + i];
+            const double rv = r[base + i] - a * q[base + i];
+            r[base + i] = rv;
+            acc += rv * rv;
+        }
+    }
+    block_add_d(acc, rr_new + b);
+}
+
 // Blocks per image for the CG kernels: about eight blocks of 256 threads per
 // SM over the whole batch (full occupancy), at most one thread per element
 // (or element pair).
@@ -819,6 +905,30 @@ int natrix_nn_cg_dir(double* d, const double* r, const double* rr_new, const dou
     const bool vec = cg_vec(per, d, r);
     k_cg_dir<<<dim3(cg_blocks(vec ? per / 2 : per, B), B), 256, 0, st>>>(d, r, rr_new, rr_old,
                                                                           (int)per, vec);
+    return launch_status();
+}
+
+int natrix_nn_cg_apply_dot(const double* d, const uint8_t* mask, int32_t B, int32_t H, int32_t W,
+                           int32_t P, double* q, double* dq, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (B < 1) return NATRIX_OK;
+    if (int rc = cg_range(B, (long)H * W)) return rc;
+    if (cudaMemsetAsync(dq, 0, (size_t)B * sizeof(double), st) != cudaSuccess)
+        return launch_status();
+    k_cg_apply_dot<<<dim3(cg_rows(H, B), B), 256, 0, st>>>(d, mask, H, W, P, q, dq);
+    return launch_status();
+}
+
+int natrix_nn_cg_update(double* x, double* r, const double* d, const double* q, const double* rr,
+                        const double* dq, double* rr_new, int32_t B, int64_t per, void* stream) {
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (B < 1 || per < 1) return NATRIX_OK;
+    if (int rc = cg_range(B, per)) return rc;
+    if (cudaMemsetAsync(rr_new, 0, (size_t)B * sizeof(double), st) != cudaSuccess)
+        return launch_status();
+    const bool vec = cg_vec(per, x, r) && cg_vec(per, d, q);
+    k_cg_update<<<dim3(cg_blocks(vec ? per / 2 : per, B), B), 256, 0, st>>>(
+        x, r, d, q, rr, dq, rr_new, (int)per, vec);
     return launch_status();
 }
 

@@ -320,6 +320,30 @@ def test_cg_kernels_match_numpy(cuda, B, H, W, offset):
                                atol=1e-14)
     np.testing.assert_allclose(dir_d.cpu().numpy().reshape(B, H, W), r + coef * d, rtol=1e-14,
                                atol=1e-14)
+    # the fused passes: q = -A d with d.q, then x += a d, r -= a q with r.r
+    # (r is 0 on obstacle cells, as in the solver)
+    rf = np.where(fluid, r, 0.0)
+    qd, dqd = dev(np.zeros_like(x)), torch.empty(B, dtype=torch.float64, device="cuda")
+    ws._call("natrix_nn_cg_apply_dot", ws._p(dd), ws._p(dm), B, H, W, P, ws._p(qd), ws._p(dqd),
+             ws._s())
+    xf, rfd = dev(x), dev(rf)
+    rr_new = torch.empty(B, dtype=torch.float64, device="cuda")
+    ws._call("natrix_nn_cg_update", ws._p(xf), ws._p(rfd), ws._p(dd), ws._p(qd), ws._p(numd),
+             ws._p(dqd), ws._p(rr_new), B, per, ws._s())
+    torch.cuda.synchronize()
+    q_np = apply_np(d)
+    dq_np = (d * q_np).sum(axis=(1, 2))
+    np.testing.assert_allclose(qd.cpu().numpy().reshape(B, H, W), q_np, rtol=1e-14, atol=1e-13)
+    np.testing.assert_allclose(dqd.cpu().numpy(), dq_np, rtol=1e-12, atol=1e-12)
+    dq_gpu = dqd.cpu().numpy()  # the coefficient the kernel used
+    a = np.where(dq_gpu != 0.0, num / np.where(dq_gpu != 0.0, dq_gpu, 1.0), 0.0).reshape(B, 1, 1)
+    r_new = rf - a * q_np
+    np.testing.assert_allclose(xf.cpu().numpy().reshape(B, H, W), x + a * d, rtol=1e-12,
+                               atol=1e-12)
+    np.testing.assert_allclose(rfd.cpu().numpy().reshape(B, H, W), r_new, rtol=1e-12,
+                               atol=1e-12)
+    np.testing.assert_allclose(rr_new.cpu().numpy(), (r_new ** 2).sum(axis=(1, 2)), rtol=1e-12,
+                               atol=1e-12)
 
 
 def test_cg_targets_reach_tolerance(cuda, oracle):
