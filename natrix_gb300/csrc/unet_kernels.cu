@@ -407,8 +407,8 @@ __global__ void __launch_bounds__(256)
                 double* __restrict__ sums /* B x 6: n, se, see, srr, sbb, pad */) {
     const int b = blockIdx.y;
     const size_t pb = (size_t)b * H * W, mb = (size_t)b * H * P;
-    // per-thread partial sums in FP32 over the thread's few pixels (the grid
-    // gives each thread about four), then FP64 for the reductions
+    // per-thread partial sums in FP32 over the thread's pixels (loss_blocks
+    // gives each thread several), float-float across the warp, FP64 after
     float fa[5] = {0, 0, 0, 0, 0};
     const int hw = H * W;
     const float scale = inv_scale[b];
@@ -424,14 +424,19 @@ __global__ void __launch_bounds__(256)
         fa[3] += r * r;
         fa[4] += bb * bb;
     }
-    // warp sums, then the block's, then one atomic per block and value (the
-    // images' 5 sums are few addresses shared by every block of the image)
+    // warp sums in float-float on the FP32 pipe (FP64 shuffles would cost
+    // every thread 25 FP64 additions), lane 0 converts; then the block's sum
+    // and one FP64 atomic per block and value
     __shared__ double part[8][5];
     const int warp = threadIdx.x >> 5;
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
-        const double v = warp_sum_d((double)fa[j]);
-        if ((threadIdx.x & 31) == 0) part[warp][j] = v;
+        FF v{fa[j], 0.0f};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v = ff_add(v, FF{__shfl_down_sync(0xffffffffu, v.h, o),
+                             __shfl_down_sync(0xffffffffu, v.l, o)});
+        if ((threadIdx.x & 31) == 0) part[warp][j] = (double)v.h + (double)v.l;
     }
     __syncthreads();
     if (threadIdx.x < 5) {
@@ -711,7 +716,7 @@ __global__ void __launch_bounds__(256)
 // Blocks per image for the CG kernels: about eight blocks of 256 threads per
 // SM over the whole batch (full occupancy), at most one thread per element
 // (or element pair).
-unsigned cg_blocks(long work_per_image, int B) {
+int sm_count() {
     static int sms = 0;
     if (!sms) {
         int dev = 0;
@@ -720,6 +725,22 @@ unsigned cg_blocks(long work_per_image, int B) {
             sms < 1)
             sms = 1;
     }
+    return sms;
+}
+
+// Blocks of 256 threads per image for the loss kernels: about 32 per SM over
+// the batch (a few waves of full occupancy), each thread looping over several
+// pixels, at most one thread per pixel.  One pixel per thread had made the
+// blocks so short that starting them (and the gradient's per-image FP64
+// constants in every block) cost more than the pixels.
+unsigned loss_blocks(long per, int B) {
+    const long want = (32L * sm_count() + B - 1) / B;
+    const long need = blocks(per, 256);
+    return (unsigned)(need < want ? need : (want > 0 ? want : 1));
+}
+
+unsigned cg_blocks(long work_per_image, int B) {
+    const int sms = sm_count();
     const long per_image = (8L * sms + B - 1) / B;
     const long need = blocks(work_per_image, 256);
     return (unsigned)(need < per_image ? need : per_image);
@@ -847,10 +868,9 @@ int natrix_nn_loss(const float* p, const float* target, const float* div, const 
     if (cudaMemsetAsync(sums, 0, (size_t)B * 6 * sizeof(double), st) != cudaSuccess)
         return launch_status();
     const long per = (long)H * W;
-    const unsigned bx = blocks(per, 256) < 256 ? blocks(per, 256) : 256;
-    k_loss_sums<<<dim3(bx, B), 256, 0, st>>>(p, target, div, inv_scale, mask, H, W, P, sums);
+    const unsigned gx = loss_blocks(per, B);
+    k_loss_sums<<<dim3(gx, B), 256, 0, st>>>(p, target, div, inv_scale, mask, H, W, P, sums);
     if (dp) {
-        const unsigned gx = blocks(per, 256) < 1024 ? blocks(per, 256) : 1024;
         k_loss_resid<<<dim3(gx, B), 256, 0, st>>>(p, div, inv_scale, mask, B, H, W, P, r);
         k_loss_grad<<<dim3(gx, B), 256, 0, st>>>(p, target, r, mask, sums, lambda, B, H, W, P, dp);
     }
