@@ -72,6 +72,7 @@ struct WgMnParams {
     int cout, c0, c1, B, H, W;
     int cpr, n_chunks;
     float* dw;
+    float* db;  // bias gradient from the ones slot, or null (separate kernel)
     int* status;
     uint32_t tmem_cols;
     uint32_t stage_bytes;  // kASlots x kXSlot + cout / 8 x kZSlot
@@ -101,6 +102,18 @@ __global__ void __launch_bounds__(kMnThreads, 1)
         umma::mbar_init(&done, (uint32_t)P.issuers);
         umma::mbar_init_fence();
         s_ok = 1;
+    }
+    // Bias gradient for free: the first chunk slot past the input channels
+    // holds bf16 ones in every stage (TMA never writes it), so its
+    // accumulator rows sum dZ over the chunk's pixels.
+    const int q_ones = q0 + q1;
+    if (P.db) {
+        const uint32_t ones = 0x3F803F80u;  // two bf16 1.0
+        for (int s = 0; s < P.stages; ++s) {
+            uint32_t* slot = reinterpret_cast<uint32_t*>(smem + s * P.stage_bytes + q_ones * kXSlot);
+            for (int k = tid; k < kXBox * 4; k += kMnThreads) slot[k] = ones;
+        }
+        umma::fence_smem_to_async();
     }
     if (warp == 1) umma::tmem_alloc(&tmem_slot, P.tmem_cols);
     umma::fence_before_sync();
@@ -201,6 +214,10 @@ __global__ void __launch_bounds__(kMnThreads, 1)
                             const int col = c + j, dxi = col / cout, co = col % cout;
                             atomicAdd(P.dw + ((size_t)co * cin + ci) * 9 + (dy + 1) * 3 + dxi, v[j]);
                         }
+                    } else if (ci == cin && P.db && dy == 0 && c >= cout && c < 2 * cout) {
+                        // the ones row of the centre tap: sum of dZ per output channel
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) atomicAdd(P.db + (c - cout + j), v[j]);
                     }
                 }
             }
@@ -306,6 +323,8 @@ int wgrad_tc(const uint16_t* dz, int cout, const uint16_t* x0, int c0, const uin
     if ((long)B * H * P.cpr >= (1L << 31)) return wg_fail(NATRIX_EINVAL, "wgrad: too many rows");
     P.n_chunks = B * H * P.cpr;
     P.dw = dw;
+    // the ones slot needs a free 8-channel slot of the 128 M rows
+    P.db = (db && c0 + c1 + 8 <= kRowsA) ? db : nullptr;
     P.status = status;
     P.issuers = 6 * cout <= 512 ? 2 : 1;
     uint32_t cols = 32;
@@ -340,7 +359,7 @@ int wgrad_tc(const uint16_t* dz, int cout, const uint16_t* x0, int c0, const uin
     k_wgrad_mn<<<grid, kMnThreads, smem, st>>>(tx0, tx1, tdz, P);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return wg_fail(NATRIX_ECUDA, cudaGetErrorString(e));
-    if (db) {
+    if (db && !P.db) {
         const int groups = 256 / (cout / 8);
         long blocks = (npix + groups - 1) / groups;
         blocks = blocks < 1024 ? blocks : 1024;
