@@ -64,6 +64,7 @@ struct RingPos {
 constexpr int kMnThreads = 224;
 constexpr int kIssuer2 = 6;  // warp of the second MMA issuer
 constexpr int kXSlot = 1152;                  // 66 pixels x 16 B, padded to 128 B
+constexpr int kXSlot3 = 3200;                 // three rows of 66 pixels x 16 B, padded
 constexpr int kZSlot = kChunkPix * 16;        // 64 pixels x 16 B
 constexpr int kASlots = kRowsA / 8;           // channel chunks of M = 128
 constexpr int kMnMaxStages = 12;
@@ -75,14 +76,27 @@ struct WgMnParams {
     float* db;  // bias gradient from the ones slot, or null (separate kernel)
     int* status;
     uint32_t tmem_cols;
-    uint32_t stage_bytes;  // kASlots x kXSlot + cout / 8 x kZSlot
+    uint32_t a_bytes;      // X part of a stage (the dZ segments follow it)
+    uint32_t stage_bytes;  // a_bytes + cout / 8 x kZSlot
     int stages;
     int issuers;  // 1 or 2 (two accumulator sets of 3 cout columns)
 };
 
+// kNine: one pass with all nine taps (needs 9 x cout x issuers TMEM
+// columns: cout 16).  Each input chunk arrives as one three-row box (rows
+// y - 1 .. y + 1, slot stride kXSlot3) and dZ once per chunk, a third of the
+// copies of the three-pass form; tap (dy, dx) reads row dy + 1 at +16 dx bytes.
+// Only the slots that hold channels (and the ones slot) are part of a stage;
+// the A operand's other M rows read whatever follows (the next stages or the
+// slack past the last one) and are never read back.
+template <bool kNine>
 __global__ void __launch_bounds__(kMnThreads, 1)
     k_wgrad_mn(const __grid_constant__ CUtensorMap tx0, const __grid_constant__ CUtensorMap tx1,
                const __grid_constant__ CUtensorMap tdz, const WgMnParams P) {
+    constexpr int kPasses = kNine ? 1 : 3;
+    constexpr int kTaps = kNine ? 9 : 3;
+    constexpr int kXRows = kNine ? 3 : 1;
+    constexpr uint32_t kSlot = kNine ? kXSlot3 : kXSlot;
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ uint64_t full[kMnMaxStages], empty[kMnMaxStages], done;
     __shared__ uint32_t tmem_slot;
@@ -91,8 +105,9 @@ __global__ void __launch_bounds__(kMnThreads, 1)
     const int cin = P.c0 + P.c1, cout = P.cout;
     const int q0 = P.c0 / 8, q1 = P.c1 / 8, qz = cout / 8;
     const uint32_t R = (uint32_t)P.stages;
-    const uint32_t a_bytes = (uint32_t)kASlots * kXSlot;
-    const uint32_t tx_bytes = (uint32_t)(q0 + q1) * (kChunkPix + 2) * 16u + (uint32_t)qz * kZSlot;
+    const uint32_t a_bytes = P.a_bytes;
+    const uint32_t tx_bytes =
+        (uint32_t)(q0 + q1) * kXBox * 16u * kXRows + (uint32_t)qz * kZSlot;
 
     if (tid == 0) {
         for (int i = 0; i < P.stages; ++i) {
@@ -110,8 +125,8 @@ __global__ void __launch_bounds__(kMnThreads, 1)
     if (P.db) {
         const uint32_t ones = 0x3F803F80u;  // two bf16 1.0
         for (int s = 0; s < P.stages; ++s) {
-            uint32_t* slot = reinterpret_cast<uint32_t*>(smem + s * P.stage_bytes + q_ones * kXSlot);
-            for (int k = tid; k < kXBox * 4; k += kMnThreads) slot[k] = ones;
+            uint32_t* slot = reinterpret_cast<uint32_t*>(smem + s * P.stage_bytes + q_ones * kSlot);
+            for (int k = tid; k < kXBox * 4 * kXRows; k += kMnThreads) slot[k] = ones;
         }
         umma::fence_smem_to_async();
     }
@@ -130,8 +145,8 @@ __global__ void __launch_bounds__(kMnThreads, 1)
     uint32_t armed = 0, armed_ph = 0;
     bool ok = true;
 
-    for (int pass = 0; pass < 3 && ch0 < ch1; ++pass) {
-        const int dy = pass - 1;
+    for (int pass = 0; pass < kPasses && ch0 < ch1; ++pass) {
+        const int dy = kNine ? 0 : pass - 1;  // kNine: rows y - 1 .. y + 1 in one box
         if (warp == 0 && lane == 0) {
             for (int ch = ch0; ch < ch1 && ok; ++ch, ps.next(R)) {
                 ok = umma::mbar_wait(&empty[ps.i], ps.ph ^ 1u);
@@ -142,10 +157,11 @@ __global__ void __launch_bounds__(kMnThreads, 1)
                 umma::mbar_arrive_expect_tx(&full[ps.i], tx_bytes);
                 armed |= 1u << ps.i;
                 armed_ph = (armed_ph & ~(1u << ps.i)) | (ps.ph << ps.i);
+                const int ty = kNine ? y - 1 : y + dy;
                 for (int q = 0; q < q0; ++q)
-                    umma::tma_load_4d(st + q * kXSlot, &tx0, 8 * q, x0 - 1, y + dy, b, &full[ps.i]);
+                    umma::tma_load_4d(st + q * kSlot, &tx0, 8 * q, x0 - 1, ty, b, &full[ps.i]);
                 for (int q = 0; q < q1; ++q)
-                    umma::tma_load_4d(st + (q0 + q) * kXSlot, &tx1, 8 * q, x0 - 1, y + dy, b,
+                    umma::tma_load_4d(st + (q0 + q) * kSlot, &tx1, 8 * q, x0 - 1, ty, b,
                                       &full[ps.i]);
                 for (int q = 0; q < qz; ++q)
                     umma::tma_load_4d(st + a_bytes + q * kZSlot, &tdz, 8 * q, x0, y, b, &full[ps.i]);
@@ -153,12 +169,12 @@ __global__ void __launch_bounds__(kMnThreads, 1)
             if (!ok) s_ok = 0;
         } else if ((warp == 1 || (warp == kIssuer2 && P.issuers == 2)) && lane == 0) {
             const int ii = warp == 1 ? 0 : 1;  // this issuer takes chunks it % issuers == ii
-            const uint32_t acc = tmem + (uint32_t)(ii * 3 * cout);
+            const uint32_t acc = tmem + (uint32_t)(ii * kTaps * cout);
             // both operands MN-major (instruction descriptor bits 15, 16)
             const uint32_t idesc = umma::idesc_bf16_f32(kRowsA, cout) | (1u << 15) | (1u << 16);
             // MN-major without swizzling: LBO = 128 B between 8-pixel groups
             // (along K), SBO = one chunk slot between 8-channel groups (M / N)
-            const uint64_t a0 = umma::smem_desc(umma::smem_u32(smem), 128, kXSlot);
+            const uint64_t a0 = umma::smem_desc(umma::smem_u32(smem), 128, kSlot);
             const uint64_t b0 = umma::smem_desc(umma::smem_u32(smem + a_bytes), 128, kZSlot);
             const uint32_t stage16 = P.stage_bytes >> 4;
             int it = 0;
@@ -170,11 +186,12 @@ __global__ void __launch_bounds__(kMnThreads, 1)
                 umma::fence_after_sync();
                 const uint64_t ab = a0 + ms.i * stage16, bb = b0 + ms.i * stage16;
 #pragma unroll
-                for (int dxi = 0; dxi < 3; ++dxi) {
+                for (int t = 0; t < kTaps; ++t) {
+                    // row t / 3 of the box (66 pixels = 66 units of 16 B), pixel shift t % 3
+                    const uint32_t aoff = (uint32_t)((t / 3) * kXBox + t % 3);
 #pragma unroll
                     for (int m = 0; m < kChunkPix / 16; ++m)
-                        umma::mma_bf16(acc + (uint32_t)(dxi * cout),
-                                       ab + (uint32_t)dxi + (uint32_t)m * 16u,
+                        umma::mma_bf16(acc + (uint32_t)(t * cout), ab + aoff + (uint32_t)m * 16u,
                                        bb + (uint32_t)m * 16u, idesc,
                                        (!first || m > 0) ? 1u : 0u);
                 }
@@ -195,7 +212,7 @@ __global__ void __launch_bounds__(kMnThreads, 1)
                 umma::fence_after_sync();
                 const int quarter = warp & 3;
                 const int ci = quarter * 32 + lane;
-                for (int c = 0; c < 3 * cout; c += 16) {
+                for (int c = 0; c < kTaps * cout; c += 16) {
                     float v[16];
                     umma::tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
                     // the second set holds a sum only when the second issuer
@@ -203,21 +220,26 @@ __global__ void __launch_bounds__(kMnThreads, 1)
                     if (P.issuers == 2 && ch1 - ch0 >= 2) {
                         float v2[16];
                         umma::tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) +
-                                            (uint32_t)(3 * cout + c),
+                                            (uint32_t)(kTaps * cout + c),
                                         v2);
 #pragma unroll
                         for (int j = 0; j < 16; ++j) v[j] += v2[j];
                     }
+                    // tap t of column c: kernel row (kNine ? t / 3 : dy + 1), column t % 3
+                    constexpr int kCentre = kNine ? 4 : 1;
                     if (ci < cin) {
 #pragma unroll
                         for (int j = 0; j < 16; ++j) {
-                            const int col = c + j, dxi = col / cout, co = col % cout;
-                            atomicAdd(P.dw + ((size_t)co * cin + ci) * 9 + (dy + 1) * 3 + dxi, v[j]);
+                            const int col = c + j, t = col / cout, co = col % cout;
+                            const int ky = kNine ? t / 3 : dy + 1;
+                            atomicAdd(P.dw + ((size_t)co * cin + ci) * 9 + ky * 3 + t % 3, v[j]);
                         }
-                    } else if (ci == cin && P.db && dy == 0 && c >= cout && c < 2 * cout) {
+                    } else if (ci == cin && P.db && dy == 0 && c >= kCentre * cout &&
+                               c < (kCentre + 1) * cout) {
                         // the ones row of the centre tap: sum of dZ per output channel
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) atomicAdd(P.db + (c - cout + j), v[j]);
+                        for (int j = 0; j < 16; ++j)
+                            atomicAdd(P.db + (c - kCentre * cout + j), v[j]);
                     }
                 }
             }
@@ -283,14 +305,15 @@ PFN_cuTensorMapEncodeTiled_v12000 wg_encode_fn() {
     return fn;
 }
 
-// 4-D map of an NHWC bf16 tensor whose box is one 8-channel chunk of a row
-// segment: {8 channels, box_w pixels, 1 row, 1 image}.
-bool encode_chunks(CUtensorMap* map, const void* base, int B, int H, int W, int C, int box_w) {
+// 4-D map of an NHWC bf16 tensor whose box is one 8-channel chunk of box_h
+// row segments: {8 channels, box_w pixels, box_h rows, 1 image}.
+bool encode_chunks(CUtensorMap* map, const void* base, int B, int H, int W, int C, int box_w,
+                   int box_h = 1) {
     auto fn = wg_encode_fn();
     if (!fn) return false;
     cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
     cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
-    cuuint32_t box[4] = {8, (cuuint32_t)box_w, 1, 1};
+    cuuint32_t box[4] = {8, (cuuint32_t)box_w, (cuuint32_t)box_h, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
     return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box,
               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -326,13 +349,21 @@ int wgrad_tc(const uint16_t* dz, int cout, const uint16_t* x0, int c0, const uin
     // the ones slot needs a free 8-channel slot of the 128 M rows
     P.db = (db && c0 + c1 + 8 <= kRowsA) ? db : nullptr;
     P.status = status;
-    P.issuers = 6 * cout <= 512 ? 2 : 1;
+    // nine taps in one pass when two issuers' accumulators fit (cout 16)
+    const bool nine = 2 * 9 * cout <= 512;
+    const int taps = nine ? 9 : 3;
+    P.issuers = 2 * taps * cout <= 512 ? 2 : 1;
     uint32_t cols = 32;
-    while (cols < (uint32_t)(3 * cout * P.issuers)) cols *= 2;
+    while (cols < (uint32_t)(taps * cout * P.issuers)) cols *= 2;
     P.tmem_cols = cols;
-    P.stage_bytes = (uint32_t)kASlots * kXSlot + (uint32_t)(cout / 8) * kZSlot;
-    const uint32_t budget = 200u * 1024u;
-    P.stages = (int)(budget / P.stage_bytes);
+    // kNine: the channel slots plus the ones slot; the A operand's other M
+    // rows reach up to 15 slots + the last tap's rows past a stage's start
+    // (51,168 bytes), covered by the reach below.  Three passes: all 16 slots.
+    P.a_bytes = nine ? (uint32_t)((c0 + c1) / 8 + 1) * kXSlot3 : (uint32_t)kASlots * kXSlot;
+    P.stage_bytes = P.a_bytes + (uint32_t)(cout / 8) * kZSlot;
+    const uint32_t reach = nine ? 51200u : 8192u;
+    const uint32_t budget = (nine ? 220u : 200u) * 1024u;
+    P.stages = (int)((budget - (nine ? reach : 0u)) / P.stage_bytes);
     if (P.stages > kMnMaxStages) P.stages = kMnMaxStages;
     // Two issuers take alternate chunks; with an even ring every stage's
     // chunks share one parity, so each stage is only ever consumed by one
@@ -343,20 +374,22 @@ int wgrad_tc(const uint16_t* dz, int cout, const uint16_t* x0, int c0, const uin
     if (P.stages < 2) return wg_fail(NATRIX_EINVAL, "wgrad: stage does not fit");
     // slack past the last stage: every descriptor read stays inside the
     // allocation whichever of its two strides runs along K
-    const uint32_t smem = (uint32_t)P.stages * P.stage_bytes + 8192u;
+    const uint32_t smem = (uint32_t)P.stages * P.stage_bytes + reach;
+    const int rows = nine ? 3 : 1;
     CUtensorMap tx0, tx1, tdz;
-    if (!encode_chunks(&tx0, x0, B, H, W, c0, kXBox) ||
-        !encode_chunks(&tx1, c1 ? x1 : x0, B, H, W, c1 ? c1 : c0, kXBox) ||
+    if (!encode_chunks(&tx0, x0, B, H, W, c0, kXBox, rows) ||
+        !encode_chunks(&tx1, c1 ? x1 : x0, B, H, W, c1 ? c1 : c0, kXBox, rows) ||
         !encode_chunks(&tdz, dz, B, H, W, cout, kChunkPix))
         return wg_fail(NATRIX_ECUDA, "wgrad: tensor map encoding failed");
-    if (cudaFuncSetAttribute(k_wgrad_mn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+    auto kernel = nine ? k_wgrad_mn<true> : k_wgrad_mn<false>;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return wg_fail(NATRIX_ECUDA, "wgrad: shared memory attribute");
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int grid = P.n_chunks < sms ? P.n_chunks : sms;
-    k_wgrad_mn<<<grid, kMnThreads, smem, st>>>(tx0, tx1, tdz, P);
+    kernel<<<grid, kMnThreads, smem, st>>>(tx0, tx1, tdz, P);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return wg_fail(NATRIX_ECUDA, cudaGetErrorString(e));
     if (db && !P.db) {

@@ -120,7 +120,8 @@ def ctypes_byref(c):
 @pytest.mark.parametrize("B,H,W,c0,c1,cout", [(2, 8, 40, 16, 0, 32), (1, 12, 24, 64, 32, 32),
                                               (2, 6, 16, 8, 0, 16), (3, 20, 70, 32, 16, 64),
                                               (2, 64, 160, 16, 8, 32), (1, 40, 200, 32, 0, 96),
-                                              (1, 6, 72, 64, 56, 16), (1, 6, 72, 64, 64, 16)])
+                                              (1, 6, 72, 64, 56, 16), (1, 6, 72, 64, 64, 16),
+                                              (2, 64, 160, 48, 0, 16)])
 def test_weight_gradient(cuda, monkeypatch, cuda_cores, B, H, W, c0, c1, cout):
     """Tensor-core path (default) and CUDA-core path against torch's FP64
     conv2d_weight and the bias gradient; the fourth shape has 4200 pixels (66
@@ -129,7 +130,10 @@ def test_weight_gradient(cuda, monkeypatch, cuda_cores, B, H, W, c0, c1, cout):
     has room for one accumulator set only.  On the tensor cores the bias
     gradient comes from a slot of bf16 ones past the input channels (the
     seventh shape, 120 channels, uses the last slot); with 128 input channels
-    (the eighth) there is no free slot and a separate kernel sums it."""
+    (the eighth) there is no free slot and a separate kernel sums it.  With
+    16 output channels all nine taps run in one pass from three-row input
+    boxes (the third, seventh, eighth and ninth shapes; the ninth gives blocks
+    several chunks for both issuers)."""
     import torch
 
     if cuda_cores:
