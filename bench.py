@@ -6,7 +6,15 @@ per step on velocity and density, density advection, dt = 1/60.  A "step" is
 one frame: obstacles, forcing, FluidSimulator.update, SmoothParticlesArea.update.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl natrix|reference]
-                  [--workload large|small]
+                  [--workload large|small|particles|batch|warmstart|unet-forward|
+                              unet-train|render|aux]
+
+The other workloads print their own line: particles (4M Lagrangian particles
+coupled to a 1024x1024 solver), batch (512 simulations of uneven size in one
+graph-captured launch per phase), warmstart (network training on solver pairs
+and the time to a residual target with and without the network's guess),
+unet-forward / unet-train (network throughput), render (display buffers) and
+aux (the kernels outside the default step, each timed at full size).
 
 One JSON line on rank 0.  `value` is timed with CUDA events on the launching
 stream with the fields resident on the device (the per-step forcing records,
