@@ -13,7 +13,6 @@ and the obstacle mask is stored as the next step will see it.
 from __future__ import annotations
 
 from pathlib import Path
-from typing import Optional
 
 import numpy as np
 

@@ -11,7 +11,6 @@ from __future__ import annotations
 import ctypes
 import json
 from pathlib import Path
-from typing import Optional
 
 import numpy as np
 import torch
