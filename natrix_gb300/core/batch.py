@@ -136,16 +136,7 @@ class FluidBatch:
             timings = []
             for cfg, spl in candidates:
                 self.set_tuning(c, cfg, spl)
-                for _ in range(2):
-                    self.step(dt)
-                ev0 = torch.cuda.Event(enable_timing=True)
-                ev1 = torch.cuda.Event(enable_timing=True)
-                ev0.record()
-                for _ in range(steps):
-                    self.step(dt)
-                ev1.record()
-                ev1.synchronize()
-                timings.append((ev0.elapsed_time(ev1) / steps, cfg, spl))
+                timings.append((self._time_steps(steps, dt), cfg, spl))
             _, cfg, spl = min(timings)
             self.set_tuning(c, cfg, spl)
             best[c] = (cfg, spl)
@@ -156,6 +147,20 @@ class FluidBatch:
             CACHE.parent.mkdir(exist_ok=True)
             CACHE.write_text(json.dumps(data, indent=1))
         return best
+
+    def _time_steps(self, steps: int, dt: float) -> float:
+        """Milliseconds per batch step with the current tuning: two untimed
+        steps, then `steps` steps between CUDA events on the current stream."""
+        for _ in range(2):
+            self.step(dt)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(steps):
+            self.step(dt)
+        ev1.record()
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1) / steps
 
     def _cache_key(self) -> str:
         name = torch.cuda.get_device_name()
