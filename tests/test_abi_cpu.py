@@ -101,3 +101,35 @@ def test_reference_import_path():
     from natrix_gb300 import FluidSimulator as B
 
     assert A is B
+
+
+def test_entry_points_validate_before_touching_the_device():
+    """Arguments the C ABI refuses come back as error codes without any
+    device call (so these run on a machine without a GPU): the no-allocation
+    residual, the weight gradient's channel rule and the CG grid limits."""
+    import ctypes
+
+    from natrix_gb300 import _lib
+    from natrix_gb300.core import warmstart as ws
+
+    lib = _lib.load()
+    nn = ws._lib_nn()
+    P = ctypes.c_void_p
+    fake = P(256)  # never dereferenced: validation fails first
+    # natrix_residual_noalloc: NULL inputs, bad sizes, grids over the static scratch
+    assert lib.natrix_residual_noalloc(None, fake, None, 8, 8, 8, fake, None) == _lib.NATRIX_EINVAL
+    assert lib.natrix_residual_noalloc(fake, fake, None, 8, 8, 4, fake, None) == _lib.NATRIX_EINVAL
+    assert lib.natrix_residual_noalloc(fake, fake, None, 8192, 8192, 8192, fake,
+                                       None) == _lib.NATRIX_ERANGE
+    assert b"static" in lib.natrix_last_error()
+    # weight gradient: channel counts must be multiples of 8
+    assert nn.natrix_nn_wgrad(fake, 12, fake, 16, None, 0, 1, 8, 8, fake, fake,
+                              None) == _lib.NATRIX_EINVAL
+    assert b"multiples of 8" in lib.natrix_last_error()
+    # CG: at most 65535 images and 2^31 cells per image
+    assert nn.natrix_nn_cg_apply(fake, None, 70000, 8, 8, 32, fake, None) == _lib.NATRIX_ERANGE
+    assert nn.natrix_nn_cg_axpy(fake, fake, fake, fake, 1.0, 2, 1 << 31, None) == _lib.NATRIX_ERANGE
+    assert nn.natrix_nn_cg_update(fake, fake, fake, fake, fake, fake, fake, 70000, 64,
+                                  None) == _lib.NATRIX_ERANGE
+    # empty batches are a no-op
+    assert nn.natrix_nn_cg_dir(fake, fake, fake, fake, 0, 64, None) == _lib.NATRIX_OK
