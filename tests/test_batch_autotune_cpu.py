@@ -82,3 +82,39 @@ def test_autotune_without_cache(tmp_path, monkeypatch):
     fb = FakeBatch([300, 400], [300, 100], cost)
     assert fb.autotune(cache=False) == {2: (2, 8)}
     assert not (tmp_path / "autotune.json").exists()
+
+
+def test_time_steps_brackets_the_timed_steps(monkeypatch):
+    """The timing itself: two untimed steps, then `steps` steps between two
+    CUDA events (a fake event class that reads a step counter here)."""
+
+    class Counting(nb.FluidBatch):
+        def __init__(self):
+            self.done = []
+            self._handle = None
+
+        def step(self, dt):
+            self.done.append(dt)
+
+        def destroy(self):
+            pass
+
+    fb = Counting()
+
+    class FakeEvent:
+        def __init__(self, enable_timing=False):
+            assert enable_timing
+            self.at = None
+
+        def record(self):
+            self.at = len(fb.done)
+
+        def synchronize(self):
+            pass
+
+        def elapsed_time(self, end):
+            return 0.5 * (end.at - self.at)  # 0.5 ms per step
+
+    monkeypatch.setattr(nb.torch.cuda, "Event", FakeEvent)
+    assert fb._time_steps(4, 0.01) == pytest.approx(0.5)
+    assert fb.done == [0.01] * 6
