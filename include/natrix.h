@@ -312,8 +312,10 @@ int natrix_quiver(const float* velocity, int32_t width, int32_t height, int64_t 
  * All calls share that array, so calls whose kernels overlap on the GPU race
  * and may return wrong sums: order them on one stream.  The first call on a
  * device looks up the array's device address (with that device current);
- * make that first call before any stream capture.  Stream-ordered on
- * `stream`; runs on the calling thread's current device. */
+ * make that first call before any stream capture.  That address is kept for
+ * the process: do not call this entry point on a device after
+ * cudaDeviceReset there.  A pitch above INT_MAX returns NATRIX_ERANGE.
+ * Stream-ordered on `stream`; runs on the calling thread's current device. */
 int natrix_residual_noalloc(const float* p, const float* div, const uint8_t* mask,
                             int32_t width, int32_t height, int64_t pitch, double* out_dev,
                             void* stream);

@@ -19,9 +19,13 @@
 // The device address of the array is looked up once per device with
 // cudaGetSymbolAddress, the first time the entry point runs on that device
 // (with that device current).  Make that first call before any stream
-// capture, since the lookup itself is not a stream operation.
+// capture, since the lookup itself is not a stream operation.  The address
+// is kept for the life of the process: after cudaDeviceReset on a device
+// (which unloads the library's device code there) the kept address is stale,
+// so do not call this entry point on that device again.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cstdio>
 #include <mutex>
 
@@ -145,11 +149,19 @@ extern "C" int natrix_residual_noalloc(const float* p, const float* div, const u
                                            "divergence or output pointer");
     if (width < 1 || height < 1 || pitch < width)
         return noalloc_fail(NATRIX_EINVAL, "natrix_residual_noalloc: bad width/height/pitch");
-    if ((long long)width * height > NATRIX_NOALLOC_MAX_CELLS || pitch > (1LL << 31)) {
+    if ((long long)width * height > NATRIX_NOALLOC_MAX_CELLS) {
         char buf[160];
         snprintf(buf, sizeof buf,
                  "natrix_residual_noalloc: %dx%d grid exceeds the %d-cell maximum of the "
                  "static scratch", width, height, NATRIX_NOALLOC_MAX_CELLS);
+        return noalloc_fail(NATRIX_ERANGE, buf);
+    }
+    // the kernel indexes rows with a 32-bit pitch
+    if (pitch > INT_MAX) {
+        char buf[160];
+        snprintf(buf, sizeof buf,
+                 "natrix_residual_noalloc: row pitch %lld exceeds the largest supported "
+                 "pitch %d", (long long)pitch, INT_MAX);
         return noalloc_fail(NATRIX_ERANGE, buf);
     }
     double* partials = nullptr;

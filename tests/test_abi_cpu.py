@@ -122,6 +122,10 @@ def test_entry_points_validate_before_touching_the_device():
     assert lib.natrix_residual_noalloc(fake, fake, None, 8192, 8192, 8192, fake,
                                        None) == _lib.NATRIX_ERANGE
     assert b"static" in lib.natrix_last_error()
+    # a row pitch the kernel's 32-bit indexing cannot hold has its own error
+    assert lib.natrix_residual_noalloc(fake, fake, None, 8, 8, 1 << 31, fake,
+                                       None) == _lib.NATRIX_ERANGE
+    assert b"pitch" in lib.natrix_last_error()
     # weight gradient: channel counts must be multiples of 8
     assert nn.natrix_nn_wgrad(fake, 12, fake, 16, None, 0, 1, 8, 8, fake, fake,
                               None) == _lib.NATRIX_EINVAL

@@ -66,4 +66,9 @@ def test_noalloc_residual_matches_handle_residual(cuda):
     rc = lib.natrix_residual_noalloc(_ptr(p), _ptr(div), None, big, 1, big, _ptr(out), sptr)
     assert rc == _lib.NATRIX_ERANGE
     assert b"maximum" in lib.natrix_last_error()
+    # so is a row pitch beyond the kernel's 32-bit row indexing (2^31 itself
+    # included); nothing is launched
+    rc = lib.natrix_residual_noalloc(_ptr(p), _ptr(div), None, W, H, 1 << 31, _ptr(out), sptr)
+    assert rc == _lib.NATRIX_ERANGE
+    assert b"pitch" in lib.natrix_last_error()
     sim.destroy()
