@@ -11,12 +11,14 @@ Differences a user can observe:
   ``update`` (the view always points at the live state buffer).
 * ``add_*`` calls are queued and applied by one fused kernel before the next
   step or field access (same results as applying them one by one).
-* Extensions with no reference counterpart: ``add_splats`` (Gaussian splat
+* Extensions with no reference counterpart: ``add_density`` (the density cone
+  splat on the attached density grids), ``add_splats`` (Gaussian splat
   forcing), ``residual``, ``jacobi``, field accessors and host copies.
 """
 from __future__ import annotations
 
 import ctypes
+import weakref
 from typing import Optional
 
 import numpy as np
@@ -81,6 +83,9 @@ class FluidSimulator:
         self._handle = ctypes.c_void_p()
         call("natrix_create", self._width, self._height, ctypes.byref(self._handle))
         self._pushed: Optional[tuple] = None
+        # density grids advected by this simulator (SmoothParticlesArea
+        # registers itself here); add_density splats into them
+        self._density_grids: list = []
 
     # ------------------------------------------------------------ properties
     @property
@@ -208,6 +213,29 @@ class FluidSimulator:
 
     # ------------------------------------------------------------- extensions
     step = update
+
+    def density_grids(self) -> list:
+        """Live density grids (SmoothParticlesArea) attached to this simulator."""
+        live = [r() for r in self._density_grids]
+        live = [d for d in live if d is not None and d._handle]
+        self._density_grids = [weakref.ref(d) for d in live]
+        return live
+
+    def add_density(self, position: tuple, value: float, radius: float):
+        """Cone splat of density (demo/shaders/shader.AddParticle.comp:18-36):
+        cells within ``radius`` cells of ``position`` (normalised) gain
+        ``value * (radius - d) / radius``, clamped to [0, 255].  Applied to
+        every density grid attached to this simulator, in its own resolution
+        (``SmoothParticlesArea.add_particles(position, radius, value)`` on
+        each); raises RuntimeError when none is attached."""
+        if not self.simulate:
+            return
+        grids = self.density_grids()
+        if not grids:
+            raise RuntimeError("add_density: no density grid (SmoothParticlesArea) is "
+                               "attached to this simulator")
+        for d in grids:
+            d.add_particles(position, radius, value)
 
     def add_splats(self, splats, density=None):
         """Gaussian splats: (n, 6) float32 {px, py, radius_cells, vx, vy, density},

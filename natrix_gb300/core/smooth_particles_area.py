@@ -8,6 +8,7 @@ is accepted and ignored.
 from __future__ import annotations
 
 import ctypes
+import weakref
 from typing import Optional
 
 import numpy as np
@@ -39,6 +40,7 @@ class SmoothParticlesArea:
         call("natrix_density_create", fluid_simulation.handle, self._width, self._height,
              ctypes.byref(self._handle))
         self._pushed: Optional[tuple] = None
+        fluid_simulation._density_grids.append(weakref.ref(self))
 
     @property
     def width(self):

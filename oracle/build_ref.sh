@@ -1,11 +1,13 @@
 #!/usr/bin/env bash
 # Compile the reference's own compute shaders (read in place from the
 # reference checkout) as C++ through the GLSL shim into oracle/_ref/.
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# The checkout is the argument, else $NATRIX_REFERENCE_ROOT, else the
+# read-only checkout this recipe was written against (/root/reference).
 # Exits 0 without building when the reference sources are absent.
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${1:-/root/reference}"
+ref="${1:-${NATRIX_REFERENCE_ROOT:-/root/reference}}"
 shaders="$ref/natrix/core/shaders/originals"
 demo="$ref/demo/shaders"
 if [ ! -f "$shaders/shader.Poisson.comp" ]; then

@@ -27,10 +27,12 @@ _LIB = _HERE / "_ref" / "libnatrix_ref.so"
 _lib = None
 
 
-def build(reference_root: str = "/root/reference") -> bool:
-    if Path(reference_root, "natrix/core/shaders/originals/shader.Poisson.comp").exists():
-        subprocess.run(["bash", str(_HERE / "build_ref.sh"), reference_root], check=True,
-                       stdout=subprocess.DEVNULL)
+def build(reference_root: str | None = None) -> bool:
+    """Compile the reference shaders with oracle/build_ref.sh (which locates the
+    checkout: `reference_root`, else NATRIX_REFERENCE_ROOT, else its default)."""
+    subprocess.run(["bash", str(_HERE / "build_ref.sh")] +
+                   ([reference_root] if reference_root else []), check=True,
+                   stdout=subprocess.DEVNULL)
     return _LIB.exists()
 
 

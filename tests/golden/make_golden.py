@@ -161,7 +161,8 @@ def steps_case(W: int, H: int, seed: int, steps: int, keep: tuple[int, ...],
 
 
 def main(argv):
-    ref_root = argv[1] if len(argv) > 1 else "/root/reference"
+    # reference checkout: argv[1], else what oracle/build_ref.sh finds
+    ref_root = argv[1] if len(argv) > 1 else None
     if not R.build(ref_root):
         raise SystemExit("reference sources not found; cannot make golden vectors")
     for (W, H, seed) in [(17, 23, 11), (64, 48, 12)]:

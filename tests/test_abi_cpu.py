@@ -101,6 +101,24 @@ def test_reference_import_path():
     from natrix_gb300 import FluidSimulator as B
 
     assert A is B
+    # the demo's density class keeps its own import path
+    # (demo/simulation_demo.py:29 of the reference)
+    from demo.smooth_particles_area import SmoothParticlesArea as C
+
+    from natrix_gb300 import SmoothParticlesArea as D
+
+    assert C is D
+
+
+def test_add_density_without_a_grid_raises():
+    from natrix_gb300 import FluidSimulator
+
+    sim = _bare(FluidSimulator)
+    sim._density_grids = []
+    with pytest.raises(RuntimeError, match="no density grid"):
+        sim.add_density((0.5, 0.5), 1.0, 2.0)
+    sim.simulate = False  # mutating calls are no-ops when simulate is False
+    sim.add_density((0.5, 0.5), 1.0, 2.0)
 
 
 def test_entry_points_validate_before_touching_the_device():

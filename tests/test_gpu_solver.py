@@ -416,6 +416,40 @@ def test_decoupled_density_grid(cuda, oracle):
     sim.destroy()
 
 
+def test_add_density_splats_attached_grids(cuda, oracle):
+    """FluidSimulator.add_density(position, value, radius) is the density cone
+    splat (demo/shaders/shader.AddParticle.comp:18-36) on every density grid
+    attached to the simulator, each in its own resolution, and it is stepped
+    with the grid like add_particles."""
+    from natrix_gb300 import FluidSimulator, SmoothParticlesArea
+
+    sim = FluidSimulator(48, 40)
+    dens = [SmoothParticlesArea(48, 40, sim), SmoothParticlesArea(96, 80, sim)]
+    ref = oracle.OracleFluid(48, 40, np.float32)
+    rdens = [oracle.OracleDensity(48, 40, ref), oracle.OracleDensity(96, 80, ref)]
+    for s in (sim, ref):
+        s.iterations, s.speed = 15, 40.0
+    for step in range(4):
+        sim.add_density((0.3 + 0.1 * step, 0.55), 120.0, 9.0)
+        for rd in rdens:
+            rd.add_particles((0.3 + 0.1 * step, 0.55), 9.0, 120.0)
+        for s in (sim, ref):
+            s.add_velocity((0.4, 0.5), (0.6, -0.2), 8.0)
+            s.update(1 / 60)
+        for d in dens + rdens:
+            d.update(1 / 60)
+    for k, (d, rd) in enumerate(zip(dens, rdens)):
+        got = d.download()
+        assert got.max() > 0
+        assert_equal_f32(got, rd.field, f"add_density grid {k}")
+    dens[1].destroy()
+    assert sim.density_grids() == [dens[0]]
+    dens[0].destroy()
+    with pytest.raises(RuntimeError, match="no density grid"):
+        sim.add_density((0.5, 0.5), 1.0, 2.0)
+    sim.destroy()
+
+
 def test_flags_borders_and_simulate(cuda, oracle):
     from natrix_gb300 import _lib
 
