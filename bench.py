@@ -68,10 +68,41 @@ BYTES = {
 
 
 def step_bytes_per_cell(spec: wl.Workload) -> int:
+    """Per-sweep-equivalent model: every kernel of the reference's dispatch
+    list (one per Jacobi sweep) reads its inputs and writes its outputs once.
+    Temporal blocking never moves most of these bytes, so this is a work
+    measure, not a bandwidth bound."""
     b = BYTES["forcing"] + BYTES["advect"] + BYTES["density_advect"] + BYTES["divergence"]
     b += BYTES["subtract_gradient"] + BYTES["jacobi_sweep"] * spec.iterations
     if spec.vorticity > 0:
         b += BYTES["vorticity_calc"] + BYTES["vorticity_apply"]
+    return b
+
+
+# Algorithmic bytes per cell of the launches this build runs (each launch
+# reads its inputs once and writes its outputs once):
+LAUNCH_BYTES = {
+    "forcing": 24,          # velocity r/w 16 + density r/w 8
+    "advect": 17,
+    "density_advect": 17,
+    "vorticity": 20,        # curl and confinement in one pass: velocity in 8 + out 8, vorticity 4
+    "divergence": 18,       # velocity 8, mask 1, divergence 4, flags 1, first sweep's pressure 4
+    "sweep_launch": 13,     # pressure 4, divergence 4, flags 1 read; pressure 4 written
+    "fused_gradient": 16,   # velocity in 8 + out 8 on the last sweep launch
+    "subtract_gradient": 21,
+}
+
+
+def step_floor_bytes_per_cell(spec: wl.Workload, sweep_launches: float, fused: float) -> float:
+    """Attainable floor of one step with the launch structure run here:
+    sweep_launches sweep launches per step, `fused` of which (0 or 1) also
+    subtract the gradient."""
+    b = (LAUNCH_BYTES["forcing"] + LAUNCH_BYTES["advect"] + LAUNCH_BYTES["density_advect"]
+         + LAUNCH_BYTES["divergence"] + LAUNCH_BYTES["sweep_launch"] * sweep_launches
+         + LAUNCH_BYTES["fused_gradient"] * fused
+         + LAUNCH_BYTES["subtract_gradient"] * (1.0 - fused))
+    if spec.vorticity > 0:
+        b += LAUNCH_BYTES["vorticity"]
     return b
 
 
@@ -85,8 +116,8 @@ def load_peaks():
 
 class ClockSampler:
     """SM clock, its maximum and the clock-event reasons during the timed
-    region: every 5 ms through NVML (ctypes on the driver's libnvidia-ml,
-    read-only queries) from a thread, or every 200 ms from nvidia-smi when
+    region: back to back (every 0.2 ms) through NVML (ctypes on the driver's
+    libnvidia-ml, read-only queries) from a thread, or every 200 ms from nvidia-smi when
     NVML cannot be loaded."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -120,12 +151,15 @@ class ClockSampler:
     def _poll(self):
         lib, h, reasons = self.nvml
         sm, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        # the maximum clock is a constant of the board: read it once, then
+        # poll the current clock and the event reasons back to back
+        if lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) != 0:
+            return
         while not self.stop.is_set():
             if (lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm)) == 0 and
-                    lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0 and
                     reasons(h, ctypes.byref(rs)) == 0):
                 self.rows.append((sm.value, mx.value, rs.value))
-            self.stop.wait(0.005)
+            self.stop.wait(0.0002)
 
     def __enter__(self):
         import threading
@@ -233,16 +267,25 @@ def cpu_run(spec: wl.Workload, steps: int, warmup: int, seed: int = 0):
 
 
 def cpu_sample_steps(spec: wl.Workload) -> int:
-    return 3 if spec.width >= 1024 else 50
+    """Frames of the cpu_baseline sample: about 10 s of CPU work."""
+    return 160 if spec.width >= 1024 else 2000
+
+
+# most frames the reference arm times (2000 x ~60 ms at 2048x2048)
+REFERENCE_MAX_STEPS = 2000
 
 
 def run_reference(args, spec):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     cells = spec.width * spec.height
-    steps = max(1, min(args.steps, cpu_sample_steps(spec)))
-    warm = max(1, min(args.warmup, 1))
+    # the same K timed frames after W warm-up frames as the GPU arm (about
+    # 60 ms per 2048x2048 frame on 16 host threads), capped so that the run
+    # stays within a few minutes
+    steps = max(1, min(args.steps, REFERENCE_MAX_STEPS))
+    warm = max(0, min(args.warmup, REFERENCE_MAX_STEPS))
     sec, threads = cpu_run(spec, steps, warm)
     value = cells / sec
     sample = f"{steps} timed frames after {warm} warm-up of the {spec.width}x{spec.height} workload"
@@ -251,7 +294,7 @@ def run_reference(args, spec):
         "unit": "cell-updates/s", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded splats and discs)",
-        "config": workload_config(spec),
+        "config": workload_config(spec, {"parallelism": f"replicas{world}"}),
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
@@ -264,33 +307,26 @@ def run_reference(args, spec):
 
 
 # ------------------------------------------------------------------ GPU leg
-def run_natrix(args, spec):
+def measure_grid(spec: wl.Workload, steps: int, warmup: int, seed: int, barrier=None,
+                 local: int = 0, sample_clocks: bool = True) -> dict:
+    """One single-grid workload through the public API: `warmup` untimed
+    frames, `steps` frames between CUDA events on the launching stream (the
+    Jacobi phases bracketed by the library's own events), then `steps` more
+    frames end to end, each with its density frame read back into pinned
+    host memory.  Returns the times and the library's launch statistics."""
     import torch
-    import torch.distributed as dist
 
     from natrix_gb300 import FluidSimulator, SmoothParticlesArea, _lib
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl")
-
-    def barrier():
-        if world > 1:
-            dist.barrier()
-
+    barrier = barrier or (lambda: None)
     W, H = spec.width, spec.height
-    cells = W * H
     sim = FluidSimulator(W, H)
     den = SmoothParticlesArea(W, H, sim)
     sim.iterations, sim.vorticity, sim.viscosity = spec.iterations, spec.vorticity, spec.viscosity
     sim.speed, sim.dissipation = spec.speed, spec.dissipation
     den.speed, den.dissipation = spec.speed, spec.dissipation
-    seed = replicas.replica_seed(rank)
     obst = wl.workload_obstacles(seed, spec)
-    total = args.warmup + 2 * args.steps
+    total = warmup + 2 * steps
     forcing = [wl.step_forcing(seed, i, spec) for i in range(total)]
     stream = torch.cuda.current_stream()
 
@@ -301,7 +337,7 @@ def run_natrix(args, spec):
         sim.update(spec.dt)
         den.update(spec.dt)
 
-    for i in range(args.warmup):
+    for i in range(warmup):
         frame(i)
     sim.sync()
     torch.cuda.synchronize()
@@ -313,9 +349,9 @@ def run_natrix(args, spec):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
+    with ClockSampler(local) if sample_clocks else _NoClocks() as clocks:
         ev0.record(stream)
-        for i in range(args.warmup, args.warmup + args.steps):
+        for i in range(warmup, warmup + steps):
             frame(i)
         ev1.record(stream)
         torch.cuda.synchronize()
@@ -324,7 +360,6 @@ def run_natrix(args, spec):
     ms = ev0.elapsed_time(ev1)
     _lib.check(lib.natrix_get_stats(sim.handle, stats, 1))
     sim.sync()
-    launches = int(stats.kernel_launches)
 
     # e2e: the same frames through the C ABI, each frame's density read back
     # into pinned host memory.  The read of frame k runs on a copy stream
@@ -339,7 +374,7 @@ def run_natrix(args, spec):
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
-    for k, i in enumerate(range(args.warmup + args.steps, total)):
+    for k, i in enumerate(range(warmup + steps, total)):
         if copied[k % 2] is not None:
             stream.wait_event(copied[k % 2])
         frame(i)
@@ -354,6 +389,43 @@ def run_natrix(args, spec):
     t_e2e = time.perf_counter() - t0
     barrier()
     sim.sync()
+    den.destroy()
+    sim.destroy()
+    return {"ms": ms, "ms_e2e": t_e2e * 1e3, "stats": stats, "clocks": clocks.summary()}
+
+
+class _NoClocks:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return False
+
+    def summary(self):
+        return None
+
+
+def run_natrix(args, spec):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    W, H = spec.width, spec.height
+    cells = W * H
+    seed = replicas.replica_seed(rank)
+    m = measure_grid(spec, args.steps, args.warmup, seed, barrier, local)
+    ms, t_e2e, stats = m["ms"], m["ms_e2e"] / 1e3, m["stats"]
+    launches = int(stats.kernel_launches)
 
     ms, ms_e2e = replicas.max_over_ranks([ms, t_e2e * 1e3], device="cuda")
     value = replicas.whole_job_rate(cells * args.steps, world, ms / 1e3)
@@ -364,13 +436,18 @@ def run_natrix(args, spec):
     jl = max(int(stats.timed_launches), 1)
     launch_ms = stats.jacobi_ms / jl
     sweeps_per_launch = stats.timed_sweeps / jl
-    # a phase whose last launch also subtracted the pressure gradient carries
-    # that kernel's bytes too
+    # Algorithmic bytes of one sweep launch: pressure, divergence and flags
+    # read once, pressure written once, whatever the number of sweeps it
+    # fuses; a launch that also subtracts the pressure gradient (the last of
+    # a step when fused) reads and writes the velocity as well.
     fused_per_launch = int(stats.timed_fused) / jl
-    alg_bytes = (BYTES["jacobi_sweep"] * sweeps_per_launch +
-                 BYTES["subtract_gradient"] * fused_per_launch) * cells
+    alg_bytes = (LAUNCH_BYTES["sweep_launch"] +
+                 LAUNCH_BYTES["fused_gradient"] * fused_per_launch) * cells
     achieved = alg_bytes / (launch_ms / 1e3) / 1e9
     traffic = load_traffic(spec)
+    sweep_launches_per_step = jl / max(int(stats.timed_phases), 1)
+    fused_per_step = int(stats.timed_fused) / max(int(stats.timed_phases), 1)
+    floor_b = step_floor_bytes_per_cell(spec, sweep_launches_per_step, fused_per_step)
 
     if rank == 0:
         # per-frame host->device bytes (carried in the launches' parameter
@@ -391,39 +468,89 @@ def run_natrix(args, spec):
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Gaussian splats and non-overlapping discs)",
             "config": workload_config(spec, {"parallelism": f"replicas{world}"}),
-            "hbm_roofline_model": {
-                "bytes_per_cell_step": step_b,
-                "achieved_gbs": value * step_b / 1e9,
-                "frac": value * step_b / 1e9 / peak,
+            # the whole step against the attainable floor of the launches it
+            # runs (each launch reads its inputs and writes its outputs once)
+            "hbm_roofline_step": {
+                "bytes_per_cell_step": floor_b,
+                "sweep_launches_per_step": sweep_launches_per_step,
+                "achieved_gbs": value * floor_b / 1e9,
+                "frac": value * floor_b / 1e9 / peak,
                 "peak_gbs": peak, "peak_kind": peak_kind,
-                "frac_of_nominal_8000": value * step_b / 1e9 / 8000.0},
+                "frac_of_nominal_8000": value * floor_b / 1e9 / 8000.0},
+            # work measure, not a bandwidth: the reference's dispatch list
+            # moves these bytes (one Jacobi dispatch per sweep)
+            "per_sweep_equivalent": {
+                "bytes_per_cell_step": step_b,
+                "gbs": value * step_b / 1e9},
             # Jacobi cell-sweeps per second: inside the step (all K sweeps of
             # every timed step over the whole step time) and inside the
             # Jacobi phase alone (sweeps over the phase's own launch time)
             "jacobi_cell_sweeps_per_s": {
                 "per_step_time": value * spec.iterations,
                 "per_jacobi_time": cells * sweeps_per_launch / (launch_ms / 1e3) * world},
-            "roofline": {"kernel": "jacobi (temporally blocked, TMA tiles)", "bound": "hbm",
+            "roofline": {"kernel": "jacobi sweep launch (temporally blocked, TMA tiles)",
+                         "bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
+                         "dram_gbs": (traffic / (launch_ms / 1e3) / 1e9) if traffic else None,
+                         "dram_frac": (traffic / (launch_ms / 1e3) / 1e9 / peak)
+                         if traffic else None,
                          "peak_kind": peak_kind,
                          "launch_ms": launch_ms, "sweeps_per_launch": sweeps_per_launch,
-                         "bytes_model": ("13 B per cell per sweep, plus 21 B per cell for the "
-                                         "gradient subtraction fused into the last launch "
-                                         "of each step" if fused_per_launch else
-                                         "13 B per cell per sweep")},
+                         "bytes_per_launch": alg_bytes,
+                         "bytes_model": ("13 B per cell per launch (pressure, divergence, "
+                                         "flags read once; pressure written once), plus "
+                                         "16 B per cell (velocity in and out) on the launch "
+                                         "that also subtracts the gradient"),
+                         "traffic_source": "profiles/jacobi_rt_%dx%d.txt" % (W, H)},
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": cells * 4},
             "gpu_launches": launches,
             "gpu_launches_per_step": launches / args.steps,
-            "clocks": clocks.summary(),
+            "clocks": m["clocks"],
             "cpu_baseline": cpu,
         }
+        if not args.no_extras and world == 1:
+            line["other_configs"] = other_configs(args)
         print(json.dumps(line), flush=True)
-    den.destroy()
-    sim.destroy()
     if world > 1:
         dist.destroy_process_group()
+
+
+def other_configs(args) -> dict:
+    """Short measurements of the other workloads, attached to the default
+    line: the 256x256 solver over its full 200 steps (with its CPU oracle
+    rate), the 4M-particle step and the 512-simulation batch (20 steps each).
+    Each is timed with CUDA events like its own bench line."""
+    out = {}
+    small = wl.SMALL_256
+    m = measure_grid(small, small.steps, 5, 0, sample_clocks=False)
+    cells = small.width * small.height
+    value = cells * small.steps / (m["ms"] / 1e3)
+    entry = {"workload": small.name, "steps": small.steps, "ms_per_step": m["ms"] / small.steps,
+             "value": value, "unit": "cell-updates/s",
+             "e2e": cells * small.steps / (m["ms_e2e"] / 1e3),
+             "gpu_launches_per_step": int(m["stats"].kernel_launches) / small.steps}
+    if not args.no_cpu:
+        csec, threads = cpu_run(small, small.steps, 1)
+        entry["cpu_baseline"] = {"value": cells / csec, "cores": threads, "kind": "port",
+                                 "sample": f"{small.steps} frames after 1 warm-up"}
+        entry["vs_cpu"] = value / (cells / csec)
+    out["small_256"] = entry
+    ns = argparse.Namespace(steps=20, warmup=5, no_cpu=True)
+    p = particles_line(ns, wl.PARTICLES_1024)
+    out["particles_4m"] = {"workload": p["config"]["workload"], "steps": 20,
+                           "ms_per_step": p["ms_per_step"], "value": p["value"],
+                           "unit": p["unit"], "coupled_frame": p["coupled_frame"]}
+    b = batch_line(ns)
+    out["batch_512"] = {k: b[k] for k in ("ms_per_step", "value", "unit",
+                                          "hbm_roofline_model", "gpu_launches_per_step")
+                        if k in b}
+    out["batch_512"]["workload"] = b["config"]["workload"]
+    out["batch_512"]["steps"] = 20
+    if "e2e" in b:
+        out["batch_512"]["e2e"] = b["e2e"]
+    return out
 
 
 def load_traffic(spec):
@@ -438,6 +565,10 @@ def load_traffic(spec):
 
 
 def run_particles(args, spec):
+    print(json.dumps(particles_line(args, spec)), flush=True)
+
+
+def particles_line(args, spec):
     """Lagrangian particles coupled to the solver: particle-steps/s of the
     particle kernel (RK2 + 3x3 splat) and of the whole coupled frame."""
     import torch
@@ -500,12 +631,16 @@ def run_particles(args, spec):
                      "atomics_per_s": 9.0 * n / (part_ms / 1e3)},
         "clocks": clocks.summary(),
     }
-    print(json.dumps(line), flush=True)
     parts.destroy()
     sim.destroy()
+    return line
 
 
 def run_batch(args):
+    print(json.dumps(batch_line(args)), flush=True)
+
+
+def batch_line(args):
     """512 independent simulations (sides 64-512, 20/40/80 sweeps, 0-6 discs,
     8 splats each per step) in one graph launch per step, against looping
     the single-grid simulator over the same simulations."""
@@ -613,7 +748,7 @@ def run_batch(args):
             "speedup_of_batch": loop_ms / ms},
         "clocks": clocks.summary(),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_warmstart(args):
@@ -1055,6 +1190,8 @@ def main():
     ap.add_argument("--solve-limit", type=float, default=120.0,
                     help="warmstart: seconds allowed per solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload: skip the short runs of the other workloads")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 500 if args.workload == "large" else 50
