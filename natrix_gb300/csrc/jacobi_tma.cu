@@ -26,6 +26,7 @@
 #include <cudaTypedefs.h>
 
 #include <cstdlib>
+#include <type_traits>
 
 #include "kernels.cuh"
 
@@ -458,14 +459,17 @@ __global__ void __launch_bounds__(C::THREADS, 1)
 
         // One sweep of row r from the old values of the rows above (up) and
         // below (dn); left / right neighbours by shuffle.
-        auto sweep_row = [&](int r, const float* up, const float* dn) {
+        // SIDE_: the tile touches a side wall (else the wall selects are dropped)
+        auto sweep_row = [&](auto SIDE_, int r, const float* up, const float* dn) {
             float cur[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) cur[j] = p[r][j];
             float lft = __shfl_up_sync(FULL, cur[3], 1);
             float rgt = __shfl_down_sync(FULL, cur[0], 1);
-            lft = wall_l ? cur[0] : lft;
-            rgt = wall_r ? cur[3] : rgt;
+            if (decltype(SIDE_)::value) {
+                lft = wall_l ? cur[0] : lft;
+                rgt = wall_r ? cur[3] : rgt;
+            }
             const float L[4] = {lft, cur[0], cur[1], cur[2]};
             const float Rn[4] = {cur[1], cur[2], cur[3], rgt};
             if (slow & (1u << r)) {
@@ -489,6 +493,7 @@ __global__ void __launch_bounds__(C::THREADS, 1)
         // the two edge rows with the neighbouring warps' rows.  Warps reach
         // the barrier after the bulk of their work, so arrival skew costs
         // less; rows 1 and R-2 keep their old values for the edge rows.
+        auto sweep_all = [&](auto SIDE_) {
         for (int s = 0; s < job.sweeps; ++s) {
             float* xs = X + (s & 1) * (C::NW * 2 * RX);
             *reinterpret_cast<float4*>(xs + (w * 2 + 0) * RX + c0) =
@@ -510,7 +515,7 @@ __global__ void __launch_bounds__(C::THREADS, 1)
                     float cur[4];
 #pragma unroll
                     for (int j = 0; j < 4; ++j) cur[j] = p[r][j];
-                    sweep_row(r, up, p[r + 1]);
+                    sweep_row(SIDE_, r, up, p[r + 1]);
 #pragma unroll
                     for (int j = 0; j < 4; ++j) up[j] = cur[j];
                 }
@@ -528,9 +533,15 @@ __global__ void __launch_bounds__(C::THREADS, 1)
                 up0[0] = a.x; up0[1] = a.y; up0[2] = a.z; up0[3] = a.w;
                 belowR[0] = b.x; belowR[1] = b.y; belowR[2] = b.z; belowR[3] = b.w;
             }
-            sweep_row(0, up0, old1);
-            sweep_row(R - 1, oldm, belowR);
+            sweep_row(SIDE_, 0, up0, old1);
+            sweep_row(SIDE_, R - 1, oldm, belowR);
         }
+        };
+        // the side-wall lanes are the same in every warp of a tile
+        if (__any_sync(FULL, wall_l || wall_r))
+            sweep_all(std::true_type{});
+        else
+            sweep_all(std::false_type{});
         const Grid& g = job.g;
         if (job.vin) {
             // Gradient subtraction on the output tile (cell_subtract_gradient's
