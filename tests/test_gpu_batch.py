@@ -137,3 +137,64 @@ def test_batch_workload_sample_matches_oracle(cuda, oracle):
         assert_equal_f32(batch.download(i, _lib.FIELD_PRESSURE), f.pressure, f"sim {i} pressure")
         assert_equal_f32(batch.download(i, _lib.FIELD_DENSITY), d.field, f"sim {i} density")
     batch.destroy()
+
+
+def test_batch_512_workload_equals_single_simulators(cuda):
+    """The whole 512-simulation workload (sides 64-512, 20/40/80 sweeps, 0-6
+    discs, 8 splats each per step) stepped as one batch with its autotuned
+    tiles and the captured graph, against 512 independently stepped
+    FluidSimulator + SmoothParticlesArea pairs driven through the same calls:
+    every simulation's velocity, pressure, divergence and density equal bit
+    for bit after 3 steps."""
+    from natrix_gb300 import FluidSimulator, SmoothParticlesArea
+    from natrix_gb300 import workloads as wl
+    from natrix_gb300.core.batch import FluidBatch
+
+    spec = wl.BATCH_512
+    sides, its = spec.sides(), spec.iterations()
+    n = spec.n_sims
+    assert n == 512
+
+    def make_batch():
+        b = FluidBatch(list(sides), list(sides))
+        for i in range(n):
+            b.set_params(i, speed=5.0, iterations=int(its[i]), dissipation=0.99,
+                         vorticity=0.0, viscosity=0.0)
+        b.set_density_params(-1, speed=5.0, dissipation=0.99)
+        return b
+
+    # tile shapes and sweeps per launch as the autotuner picks them (timed on
+    # a batch of its own, so the compared batch starts from rest)
+    tuner = make_batch()
+    tuning = tuner.autotune(cache=False)
+    tuner.destroy()
+    batch = make_batch()
+    for c, (cfg, spl) in tuning.items():
+        batch.set_tuning(c, cfg, spl)
+    singles = []
+    for i in range(n):
+        s = FluidSimulator(int(sides[i]), int(sides[i]))
+        d = SmoothParticlesArea(int(sides[i]), int(sides[i]), s)
+        s.speed, s.iterations, s.dissipation, s.vorticity, s.viscosity = (
+            5.0, int(its[i]), 0.99, 0.0, 0.0)
+        d.speed, d.dissipation = 5.0, 0.99
+        singles.append((s, d))
+    obst = [spec.obstacles(i, int(sides[i])) for i in range(n)]
+    for step in range(3):
+        for i in range(n):
+            s, d = singles[i]
+            for o in obst[i]:
+                batch.add_circle_obstacle(i, (float(o[0]), float(o[1])), float(o[2]))
+                s.add_circle_obstacle((float(o[0]), float(o[1])), float(o[2]))
+            spl = spec.forcing(i, step, int(sides[i]))
+            batch.add_splats(i, spl)
+            s.add_splats(spl, d)
+        batch.step(1 / 60)
+        for s, d in singles:
+            s.update(1 / 60)
+            d.update(1 / 60)
+    compare(batch, singles)
+    batch.destroy()
+    for s, d in singles:
+        d.destroy()
+        s.destroy()
