@@ -52,18 +52,19 @@ __device__ __forceinline__ bool disc_meets_box(float cx, float cy, float r, int 
     return dx * dx + dy * dy <= rr * rr;
 }
 
-// ROWS: rows of cells per thread (the block covers BX x BY*ROWS cells, the
-// shape list is loaded and culled once for all of them).
-template <int ROWS = 1>
+// ROWS: rows of cells per thread (the block covers BX x TBY*ROWS cells, the
+// shape list is loaded and culled once for all of them); the block has BX x
+// TBY threads.
+template <int ROWS = 1, int TBY = BY>
 __device__ __forceinline__ void block_obstacles(uint8_t* __restrict__ mask, Grid g,
                                                 const ShapeOp* __restrict__ ops, int n, int fresh,
                                                 int bx0, int by0) {
     __shared__ ShapeOp s_ops[kMaxOpsPerLaunch];
     __shared__ int s_kept[kMaxOpsPerLaunch];
     const int tid = threadIdx.y * BX + threadIdx.x;
-    for (int i = tid; i < n; i += BX * BY) s_ops[i] = ops[i];
+    for (int i = tid; i < n; i += BX * TBY) s_ops[i] = ops[i];
     __syncthreads();
-    const int bx1 = bx0 + BX - 1, by1 = by0 + BY * ROWS - 1;
+    const int bx1 = bx0 + BX - 1, by1 = by0 + TBY * ROWS - 1;
     const int nk = cull_ops(n, s_kept, [&](int k) {
         const ShapeOp& op = s_ops[k];
         // triangles are never culled: the reference's same-sign test marks
@@ -77,7 +78,7 @@ __device__ __forceinline__ void block_obstacles(uint8_t* __restrict__ mask, Grid
     if (x >= g.W) return;
 #pragma unroll
     for (int r = 0; r < ROWS; ++r) {
-        const int y = by0 + threadIdx.y + r * BY;
+        const int y = by0 + threadIdx.y + r * TBY;
         if (y >= g.H) break;
         const size_t i = (size_t)y * g.P + x;
         uint8_t m = fresh ? 0 : mask[i];
@@ -121,7 +122,7 @@ __device__ __forceinline__ bool op_is_velocity(int kind) {
 // zero (shader.InitBoundaries.comp, which the reference dispatches next when
 // the step starts); only meaningful when the list holds a velocity op, since
 // then every cell is written.
-template <int ROWS = 1>
+template <int ROWS = 1, int TBY = BY, bool CG = false>
 __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
                                               float* __restrict__ rho, Grid gd,
                                               const ForceOp* __restrict__ ops, int n, int bx0,
@@ -135,14 +136,14 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
     if (vel) {
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) {
-            const int y = by0 + threadIdx.y + r * BY;
-            if (x < gv.W && y < gv.H) va[r] = vel[(size_t)y * gv.P + x];
+            const int y = by0 + threadIdx.y + r * TBY;
+            if (x < gv.W && y < gv.H) va[r] = ldp<CG>(vel + (size_t)y * gv.P + x);
         }
     }
     const int tid = threadIdx.y * BX + threadIdx.x;
-    for (int i = tid; i < n; i += BX * BY) s_ops[i] = ops[i];
+    for (int i = tid; i < n; i += BX * TBY) s_ops[i] = ops[i];
     __syncthreads();
-    const int bx1 = bx0 + BX - 1, by1 = by0 + BY * ROWS - 1;
+    const int bx1 = bx0 + BX - 1, by1 = by0 + TBY * ROWS - 1;
     if (vel) {
         int first_vel = -1;
         for (int k = 0; k < n; ++k)
@@ -162,7 +163,7 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
         });
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) {
-            const int y = by0 + threadIdx.y + r * BY;
+            const int y = by0 + threadIdx.y + r * TBY;
             if (first_vel < 0 || x >= gv.W || y >= gv.H) continue;
             const size_t i = (size_t)y * gv.P + x;
             float2 a = va[r];
@@ -222,12 +223,12 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
         float ra[ROWS];
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) {
-            const int y = by0 + threadIdx.y + r * BY;
-            if (nk != 0 && x < gd.W && y < gd.H) ra[r] = rho[(size_t)y * gd.P + x];
+            const int y = by0 + threadIdx.y + r * TBY;
+            if (nk != 0 && x < gd.W && y < gd.H) ra[r] = ldp<CG>(rho + (size_t)y * gd.P + x);
         }
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) {
-            const int y = by0 + threadIdx.y + r * BY;
+            const int y = by0 + threadIdx.y + r * TBY;
             if (nk == 0 || x >= gd.W || y >= gd.H) continue;
             const size_t i = (size_t)y * gd.P + x;
             float a = ra[r];
@@ -257,35 +258,50 @@ __device__ __forceinline__ void block_forcing(float2* __restrict__ vel, Grid gv,
 // shader.AdvectVelocity.comp:19-51, with shader.InitBoundaries.comp:11-35
 // fused: the reference zeroes the border of the read buffer in place before
 // advecting, so border cells read as zero here (centre and gathers alike).
+// CG: loads through L2 (see ldf in common.cuh).
+template <bool CG = false>
 __device__ __forceinline__ float2 vel_at(const float2* __restrict__ v, const Grid& g, int x,
                                          int y, bool zero_border) {
     if (zero_border && (x == 0 || x == g.W - 1 || y == 0 || y == g.H - 1))
         return make_float2(0.0f, 0.0f);
-    return __ldg(v + (size_t)y * g.P + x);
+    return ldf<CG>(v + (size_t)y * g.P + x);
 }
 
+// Backtrace position of a cell from its own velocity.
+__device__ __forceinline__ Corners advect_corners(float2 vel, int x, int y, const Grid& g,
+                                                  const StepParams* __restrict__ sp) {
+    const float dt = sp->dt, speed = sp->speed;
+    const float fx = (float)x - vel.x * dt * speed;
+    const float fy = (float)y - vel.y * dt * speed;
+    return corners(fx, fy, g.W, g.H);
+}
+
+// The arithmetic after the bilinear gathers (shader.AdvectVelocity.comp:38-50).
+__device__ __forceinline__ float2 advect_mix(float2 lt, float2 rt, float2 lb, float2 rb,
+                                             const Corners& c, float diss) {
+    const float h1x = mixf(lt.x, rt.x, c.dx), h1y = mixf(lt.y, rt.y, c.dx);
+    const float h2x = mixf(lb.x, rb.x, c.dx), h2y = mixf(lb.y, rb.y, c.dx);
+    const float sx = mixf(h2x, h1x, c.dy), sy = mixf(h2y, h1y, c.dy);
+    return make_float2(clampf(sx * diss, -1.0f, 1.0f), clampf(sy * diss, -1.0f, 1.0f));
+}
+
+template <bool CG = false>
 __device__ __forceinline__ void cell_advect(const float2* __restrict__ vin, float2* __restrict__ vout,
              const uint8_t* __restrict__ mask, Grid g, const StepParams* __restrict__ sp, int x, int y) {
     if (x >= g.W || y >= g.H) return;
     const size_t i = (size_t)y * g.P + x;
     const bool zb = sp->has_borders != 0;
-    if (!sp->mask_zero && mask[i]) {
+    if (!sp->mask_zero && ldp<CG>(mask + i)) {
         vout[i] = make_float2(0.0f, 0.0f);
         return;
     }
-    const float dt = sp->dt, speed = sp->speed, diss = sp->dissipation;
-    const float2 vel = vel_at(vin, g, x, y, zb);
-    const float fx = (float)x - vel.x * dt * speed;
-    const float fy = (float)y - vel.y * dt * speed;
-    const Corners c = corners(fx, fy, g.W, g.H);
-    const float2 lt = vel_at(vin, g, c.lo_x, c.hi_y, zb);
-    const float2 rt = vel_at(vin, g, c.hi_x, c.hi_y, zb);
-    const float2 lb = vel_at(vin, g, c.lo_x, c.lo_y, zb);
-    const float2 rb = vel_at(vin, g, c.hi_x, c.lo_y, zb);
-    const float h1x = mixf(lt.x, rt.x, c.dx), h1y = mixf(lt.y, rt.y, c.dx);
-    const float h2x = mixf(lb.x, rb.x, c.dx), h2y = mixf(lb.y, rb.y, c.dx);
-    const float sx = mixf(h2x, h1x, c.dy), sy = mixf(h2y, h1y, c.dy);
-    vout[i] = make_float2(clampf(sx * diss, -1.0f, 1.0f), clampf(sy * diss, -1.0f, 1.0f));
+    const float2 vel = vel_at<CG>(vin, g, x, y, zb);
+    const Corners c = advect_corners(vel, x, y, g, sp);
+    const float2 lt = vel_at<CG>(vin, g, c.lo_x, c.hi_y, zb);
+    const float2 rt = vel_at<CG>(vin, g, c.hi_x, c.hi_y, zb);
+    const float2 lb = vel_at<CG>(vin, g, c.lo_x, c.lo_y, zb);
+    const float2 rb = vel_at<CG>(vin, g, c.hi_x, c.lo_y, zb);
+    vout[i] = advect_mix(lt, rt, lb, rb, c, sp->dissipation);
 }
 
 // Clamped neighbour coordinates (natrix/core/shaders/originals/common.sh:9-19).
@@ -317,21 +333,23 @@ __device__ __forceinline__ Nbr nbrs_at(const Grid& g, int x, int y) {
 
 // ------------------------------------------------------ vorticity confinement
 // shader.CalcVorticity.comp:13-27.
+template <bool CG = false>
 __device__ __forceinline__ void cell_calc_vorticity(const float2* __restrict__ v, float* __restrict__ w, Grid g, int x, int y) {
     if (x >= g.W || y >= g.H) return;
     const Nbr n = nbrs(g, x, y);
-    const float2 vl = __ldg(v + n.l), vr = __ldg(v + n.r), vb = __ldg(v + n.b),
-                 vt = __ldg(v + n.t);
+    const float2 vl = ldf<CG>(v + n.l), vr = ldf<CG>(v + n.r), vb = ldf<CG>(v + n.b),
+                 vt = ldf<CG>(v + n.t);
     w[n.c] = 0.5f * ((vr.y - vl.y) - (vt.x - vb.x));
 }
 
 // shader.ApplyVorticity.comp:19-40.
+template <bool CG = false>
 __device__ __forceinline__ void cell_apply_vorticity(const float2* __restrict__ vin, float2* __restrict__ vout,
                       const float* __restrict__ w, Grid g, const StepParams* __restrict__ sp, int x, int y) {
     if (x >= g.W || y >= g.H) return;
     const Nbr n = nbrs(g, x, y);
-    const float wl = __ldg(w + n.l), wr = __ldg(w + n.r), wb = __ldg(w + n.b),
-                wt = __ldg(w + n.t), wc = __ldg(w + n.c);
+    const float wl = ldf<CG>(w + n.l), wr = ldf<CG>(w + n.r), wb = ldf<CG>(w + n.b),
+                wt = ldf<CG>(w + n.t), wc = ldf<CG>(w + n.c);
     float fx = 0.5f * (fabsf(wt) - fabsf(wb));
     float fy = 0.5f * (fabsf(wr) - fabsf(wl));
     const float eps = 2.4414e-4f;
@@ -344,19 +362,20 @@ __device__ __forceinline__ void cell_apply_vorticity(const float2* __restrict__ 
     fx = fx * (s * 1.0f);
     fy = fy * (s * -1.0f);
     const float dt = sp->dt;
-    const float2 v = vin[n.c];
+    const float2 v = ldp<CG>(vin + n.c);
     vout[n.c] = make_float2(v.x + fx * dt, v.y + fy * dt);
 }
 
 // ---------------------------------------------------------------- viscosity
 // shader.Viscosity.comp:17-32, one smoothing sweep.
+template <bool CG = false>
 __device__ __forceinline__ void cell_viscosity(const float2* __restrict__ vin, float2* __restrict__ vout, Grid g,
                 const StepParams* __restrict__ sp, int x, int y) {
     if (x >= g.W || y >= g.H) return;
     const Nbr n = nbrs(g, x, y);
     const float alpha = sp->alpha, rbeta = sp->rbeta;
-    const float2 a = __ldg(vin + n.l), b = __ldg(vin + n.r), c = __ldg(vin + n.b),
-                 d = __ldg(vin + n.t), e = __ldg(vin + n.c);
+    const float2 a = ldf<CG>(vin + n.l), b = ldf<CG>(vin + n.r), c = ldf<CG>(vin + n.b),
+                 d = ldf<CG>(vin + n.t), e = ldf<CG>(vin + n.c);
     vout[n.c] = make_float2((a.x + b.x + c.x + d.x + e.x * alpha) * rbeta,
                             (a.y + b.y + c.y + d.y + e.y * alpha) * rbeta);
 }
@@ -367,52 +386,100 @@ __device__ __forceinline__ void cell_viscosity(const float2* __restrict__ vin, f
 // with p = 0 everywhere, shader.Poisson.comp:37 gives (0+0+0+0 - b)*0.25,
 // which is (0 - b)*0.25 bit for bit; the reference's clear of the pressure
 // buffer (fluid_simulator.py:235-248) is thereby folded away.
+__device__ __forceinline__ float divergence_of(float x1, float x2, float y1, float y2) {
+    return 0.5f * ((x2 - x1) + (y2 - y1));
+}
+
+// Neighbour-substitution flags of a cell: wall or obstacle neighbour.
+__device__ __forceinline__ uint8_t nb_flags(int x, int y, const Grid& g, bool ol, bool orr,
+                                            bool ob, bool ot) {
+    uint8_t f = 0;
+    if (x == 0 || ol) f |= NB_L;
+    if (x == g.W - 1 || orr) f |= NB_R;
+    if (y == 0 || ob) f |= NB_B;
+    if (y == g.H - 1 || ot) f |= NB_T;
+    return f;
+}
+
+template <bool CG = false>
 __device__ __forceinline__ void cell_divergence(const float2* __restrict__ v, const uint8_t* __restrict__ mask,
                  float* __restrict__ div, uint8_t* __restrict__ flags, float* __restrict__ p1,
                  Grid g, const StepParams* __restrict__ sp, int x, int y) {
     if (x >= g.W || y >= g.H) return;
     const Nbr n = nbrs(g, x, y);
     const bool mz = sp->mask_zero != 0;
-    const bool ol = !mz && mask[n.l], orr = !mz && mask[n.r];
-    const bool ob = !mz && mask[n.b], ot = !mz && mask[n.t];
-    const float x1 = ol ? 0.0f : __ldg(v + n.l).x;
-    const float x2 = orr ? 0.0f : __ldg(v + n.r).x;
-    const float y1 = ob ? 0.0f : __ldg(v + n.b).y;
-    const float y2 = ot ? 0.0f : __ldg(v + n.t).y;
-    const float b = 0.5f * ((x2 - x1) + (y2 - y1));
+    const bool ol = !mz && ldp<CG>(mask + n.l), orr = !mz && ldp<CG>(mask + n.r);
+    const bool ob = !mz && ldp<CG>(mask + n.b), ot = !mz && ldp<CG>(mask + n.t);
+    const float x1 = ol ? 0.0f : ldf<CG>(v + n.l).x;
+    const float x2 = orr ? 0.0f : ldf<CG>(v + n.r).x;
+    const float y1 = ob ? 0.0f : ldf<CG>(v + n.b).y;
+    const float y2 = ot ? 0.0f : ldf<CG>(v + n.t).y;
+    const float b = divergence_of(x1, x2, y1, y2);
     div[n.c] = b;
-    uint8_t f = 0;
-    if (x == 0 || ol) f |= NB_L;
-    if (x == g.W - 1 || orr) f |= NB_R;
-    if (y == 0 || ob) f |= NB_B;
-    if (y == g.H - 1 || ot) f |= NB_T;
-    flags[n.c] = f;
+    flags[n.c] = nb_flags(x, y, g, ol, orr, ob, ot);
     if (p1) p1[n.c] = (0.0f - b) * 0.25f;
 }
 
 // -------------------------------------------------------- gradient subtract
 // shader.SubtractGradient.comp:17-47 (same neighbour rule as the sweep).
+__device__ __forceinline__ float2 subtract_gradient_of(float2 vel, uint8_t f, float pc, float pl,
+                                                       float pr, float pb, float pt) {
+    const float x1 = (f & NB_L) ? pc : pl;
+    const float x2 = (f & NB_R) ? pc : pr;
+    const float y1 = (f & NB_B) ? pc : pb;
+    const float y2 = (f & NB_T) ? pc : pt;
+    vel.x -= 0.5f * (x2 - x1);
+    vel.y -= 0.5f * (y2 - y1);
+    return vel;
+}
+
+template <bool CG = false>
 __device__ __forceinline__ void cell_subtract_gradient(const float2* __restrict__ vin, float2* __restrict__ vout,
                         const float* __restrict__ p, const uint8_t* __restrict__ flags,
                         Grid g, int x, int y) {
     if (x >= g.W || y >= g.H) return;
     const Nbr n = nbrs(g, x, y);
-    const uint8_t f = flags[n.c];
-    const float pc = __ldg(p + n.c);
-    const float x1 = (f & NB_L) ? pc : __ldg(p + n.l);
-    const float x2 = (f & NB_R) ? pc : __ldg(p + n.r);
-    const float y1 = (f & NB_B) ? pc : __ldg(p + n.b);
-    const float y2 = (f & NB_T) ? pc : __ldg(p + n.t);
-    float2 vel = vin[n.c];
-    vel.x -= 0.5f * (x2 - x1);
-    vel.y -= 0.5f * (y2 - y1);
-    vout[n.c] = vel;
+    const uint8_t f = ldp<CG>(flags + n.c);
+    const float pc = ldf<CG>(p + n.c);
+    const float pl = (f & NB_L) ? pc : ldf<CG>(p + n.l);
+    const float pr = (f & NB_R) ? pc : ldf<CG>(p + n.r);
+    const float pb = (f & NB_B) ? pc : ldf<CG>(p + n.b);
+    const float pt = (f & NB_T) ? pc : ldf<CG>(p + n.t);
+    vout[n.c] = subtract_gradient_of(ldp<CG>(vin + n.c), f, pc, pl, pr, pb, pt);
 }
 
 // --------------------------------------------------------- density advection
 // demo/shaders/shader.AdvectParticle.comp:21-71: the density grid (its own
 // size) is advected by the velocity sampled at the matching position of the
 // velocity grid, scaled by the grid-size ratio.
+__device__ __forceinline__ Corners density_vel_corners(int x, int y, const Grid& gd,
+                                                       const Grid& gv) {
+    const float nx = (float)x / (float)gd.W * (float)gv.W;
+    const float ny = (float)y / (float)gd.H * (float)gv.H;
+    return corners(nx, ny, gv.W, gv.H);
+}
+
+// On a cell centre (equal grid sizes) the four corners are one cell and the
+// bilinear mix of a finite velocity returns it (a -0 comes back as +0, which
+// the backtrace x - u*dt*speed cannot tell apart), so one load gives the same
+// result.
+__device__ __forceinline__ bool on_centre(const Corners& cv) {
+    return cv.lo_x == cv.hi_x && cv.lo_y == cv.hi_y && cv.dx == 0.0f && cv.dy == 0.0f;
+}
+
+// Backtrace position in the density grid from the sampled velocity.
+__device__ __forceinline__ Corners density_corners(float2 u, int x, int y, const Grid& gd,
+                                                   const Grid& gv,
+                                                   const StepParams* __restrict__ sp) {
+    u.x = u.x * ((float)gd.W / (float)gv.W);
+    u.y = u.y * ((float)gd.H / (float)gv.H);
+    const float dt = sp->dt, speed = sp->d_speed;
+    const float fx = (float)x - u.x * dt * speed;
+    const float fy = (float)y - u.y * dt * speed;
+    return corners(fx, fy, gd.W, gd.H);
+}
+
+template <bool CG = false>
 __device__ __forceinline__ void cell_density_advect(const float* __restrict__ rin, float* __restrict__ rout, Grid gd,
                      const float2* __restrict__ v, const uint8_t* __restrict__ mask, Grid gv,
                      const StepParams* __restrict__ sp, int x, int y) {
@@ -422,26 +489,16 @@ __device__ __forceinline__ void cell_density_advect(const float* __restrict__ ri
     const float ny = (float)y / (float)gd.H * (float)gv.H;
     if (!sp->mask_zero) {
         const size_t oi = (size_t)(unsigned)ny * gv.P + (unsigned)nx;
-        if (mask[oi]) {
+        if (ldp<CG>(mask + oi)) {
             rout[i] = 0.0f;
             return;
         }
     }
-    const Corners cv = corners(nx, ny, gv.W, gv.H);
-    // On a cell centre (equal grid sizes) the four corners are one cell and
-    // the bilinear mix of a finite velocity returns it (a -0 comes back as
-    // +0, which the backtrace x - u*dt*speed cannot tell apart), so one load
-    // gives the same result.
-    float2 u = (cv.lo_x == cv.hi_x && cv.lo_y == cv.hi_y && cv.dx == 0.0f && cv.dy == 0.0f)
-                   ? __ldg(v + (size_t)cv.lo_y * gv.P + cv.lo_x)
-                   : sample_vel(v, gv.P, cv);
-    u.x = u.x * ((float)gd.W / (float)gv.W);
-    u.y = u.y * ((float)gd.H / (float)gv.H);
-    const float dt = sp->dt, speed = sp->d_speed;
-    const float fx = (float)x - u.x * dt * speed;
-    const float fy = (float)y - u.y * dt * speed;
-    const Corners c = corners(fx, fy, gd.W, gd.H);
-    rout[i] = sample_scalar(rin, gd.P, c) * sp->d_dissipation;
+    const Corners cv = density_vel_corners(x, y, gd, gv);
+    const float2 u = on_centre(cv) ? ldf<CG>(v + (size_t)cv.lo_y * gv.P + cv.lo_x)
+                                   : sample_vel<CG>(v, gv.P, cv);
+    const Corners c = density_corners(u, x, y, gd, gv, sp);
+    rout[i] = sample_scalar<CG>(rin, gd.P, c) * sp->d_dissipation;
 }
 
 }  // namespace natrix

@@ -54,23 +54,48 @@ __device__ __forceinline__ Corners corners(float fx, float fy, int W, int H) {
     return c;
 }
 
+// Loads of solver fields.  A kernel that only reads a field during its
+// launch takes the read-only path (ld.global.nc, CG = false); the batch step
+// kernel, whose phases read fields that other CTAs wrote earlier in the same
+// launch, reads through L2 (ld.global.cg, CG = true), which is coherent
+// across SMs.
+template <bool CG, class T>
+__device__ __forceinline__ T ldf(const T* p) {
+    if constexpr (CG)
+        return __ldcg(p);
+    else
+        return __ldg(p);
+}
+
+// A plain load (CG = false) or an L2 load (CG = true): for the reads the
+// per-phase kernels issue as ordinary loads.
+template <bool CG, class T>
+__device__ __forceinline__ T ldp(const T* p) {
+    if constexpr (CG)
+        return __ldcg(p);
+    else
+        return *p;
+}
+
+template <bool CG = false>
 __device__ __forceinline__ float2 sample_vel(const float2* __restrict__ v, int P,
                                              const Corners& c) {
-    const float2 lt = __ldg(v + (size_t)c.hi_y * P + c.lo_x);
-    const float2 rt = __ldg(v + (size_t)c.hi_y * P + c.hi_x);
-    const float2 lb = __ldg(v + (size_t)c.lo_y * P + c.lo_x);
-    const float2 rb = __ldg(v + (size_t)c.lo_y * P + c.hi_x);
+    const float2 lt = ldf<CG>(v + (size_t)c.hi_y * P + c.lo_x);
+    const float2 rt = ldf<CG>(v + (size_t)c.hi_y * P + c.hi_x);
+    const float2 lb = ldf<CG>(v + (size_t)c.lo_y * P + c.lo_x);
+    const float2 rb = ldf<CG>(v + (size_t)c.lo_y * P + c.hi_x);
     const float h1x = mixf(lt.x, rt.x, c.dx), h1y = mixf(lt.y, rt.y, c.dx);
     const float h2x = mixf(lb.x, rb.x, c.dx), h2y = mixf(lb.y, rb.y, c.dx);
     return make_float2(mixf(h2x, h1x, c.dy), mixf(h2y, h1y, c.dy));
 }
 
+template <bool CG = false>
 __device__ __forceinline__ float sample_scalar(const float* __restrict__ s, int P,
                                                const Corners& c) {
-    const float lt = __ldg(s + (size_t)c.hi_y * P + c.lo_x);
-    const float rt = __ldg(s + (size_t)c.hi_y * P + c.hi_x);
-    const float lb = __ldg(s + (size_t)c.lo_y * P + c.lo_x);
-    const float rb = __ldg(s + (size_t)c.lo_y * P + c.hi_x);
+    const float lt = ldf<CG>(s + (size_t)c.hi_y * P + c.lo_x);
+    const float rt = ldf<CG>(s + (size_t)c.hi_y * P + c.hi_x);
+    const float lb = ldf<CG>(s + (size_t)c.lo_y * P + c.lo_x);
+    const float rb = ldf<CG>(s + (size_t)c.lo_y * P + c.hi_x);
     const float h1 = mixf(lt, rt, c.dx);
     const float h2 = mixf(lb, rb, c.dx);
     return mixf(h2, h1, c.dy);
