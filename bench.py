@@ -642,8 +642,9 @@ def run_batch(args):
 
 def batch_line(args):
     """512 independent simulations (sides 64-512, 20/40/80 sweeps, 0-6 discs,
-    8 splats each per step) in one graph launch per step, against looping
-    the single-grid simulator over the same simulations."""
+    8 splats each per step) in one persistent launch per step, against one
+    graph-replayed launch per phase and against looping the single-grid
+    simulator over the same simulations."""
     import torch
 
     from natrix_gb300 import FluidSimulator, SmoothParticlesArea
@@ -665,7 +666,6 @@ def batch_line(args):
         batch.set_params(i, speed=5.0, iterations=int(its[i]), dissipation=0.99, vorticity=0.0,
                          viscosity=0.0)
     batch.set_density_params(-1, speed=5.0, dissipation=0.99)
-    tuning = batch.autotune()
     stream = torch.cuda.current_stream()
 
     def frame(k):
@@ -673,22 +673,34 @@ def batch_line(args):
         batch.add_splats_bulk(fcounts, forcing[k])
         batch.step(1 / 60)
 
-    for k in range(args.warmup):
-        frame(k)
-    batch.sync()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
-        e0.record(stream)
-        for k in range(args.warmup, total_steps):
+    def timed(sample_clocks):
+        for k in range(args.warmup):
             frame(k)
-        e1.record(stream)
+        batch.sync()
         torch.cuda.synchronize()
-    batch.sync()
-    ms = e0.elapsed_time(e1) / args.steps
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) if sample_clocks \
+                else _NoClocks() as clocks:
+            e0.record(stream)
+            for k in range(args.warmup, total_steps):
+                frame(k)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        batch.sync()
+        return e0.elapsed_time(e1) / args.steps, clocks.summary()
+
+    # the step as one persistent launch (default), then the same work as one
+    # graph-replayed launch per phase for comparison
+    batch.use_persistent(True)
+    tuning = batch.autotune()
+    ms, clock_summary = timed(True)
+    launches_total, per_step = batch.launches()
+    batch.use_persistent(False)
+    tuning_phased = batch.autotune()
+    ms_phased, _ = timed(False)
+    _, per_step_phased = batch.launches()
     cells = float((sides.astype(np.float64) ** 2).sum())
     model_bytes = float(((sides.astype(np.float64) ** 2) * (92 + 13 * its)).sum())
-    launches_total, per_step = batch.launches()
     batch.destroy()
 
     # looping the single-grid simulator over the same simulations
@@ -743,10 +755,14 @@ def batch_line(args):
                                "frac": model_bytes / (ms / 1e3) / 1e9 / peak, "peak_gbs": peak,
                                "peak_kind": peak_kind},
         "gpu_launches_per_step": per_step,
+        "launch_per_phase": {"ms_per_step": ms_phased, "value": cells / (ms_phased / 1e3),
+                             "gpu_launches_per_step": per_step_phased,
+                             "tuning": {str(c): list(v) for c, v in tuning_phased.items()},
+                             "speedup_of_persistent": ms_phased / ms},
         "looped_single_grid": None if loop_ms is None else {
             "ms_per_step": loop_ms, "value": cells / (loop_ms / 1e3),
             "speedup_of_batch": loop_ms / ms},
-        "clocks": clocks.summary(),
+        "clocks": clock_summary,
     }
     return line
 

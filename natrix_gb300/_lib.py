@@ -99,6 +99,7 @@ SIGNATURES = {
     "natrix_batch_set_density_params": [_vp, _i, _f, _f],
     "natrix_batch_set_tuning": [_vp, _i, _i, _i],
     "natrix_batch_set_graph": [_vp, _i],
+    "natrix_batch_set_persistent": [_vp, _i],
     "natrix_batch_add_velocity": [_vp, _i, _f, _f, _f, _f, _f],
     "natrix_batch_add_splats": [_vp, _i, _vp, _i],
     "natrix_batch_add_circle_obstacle": [_vp, _i, _f, _f, _f, _i],

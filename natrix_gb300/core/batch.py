@@ -42,6 +42,7 @@ class FluidBatch:
         self._handle = ctypes.c_void_p()
         call("natrix_batch_create", self.n, w, h, ctypes.byref(self._handle))
         self.tuning = {}
+        self.persistent = True
 
     @property
     def handle(self):
@@ -66,6 +67,11 @@ class FluidBatch:
 
     def use_graph(self, enable: bool):
         call("natrix_batch_set_graph", self.handle, 1 if enable else 0)
+
+    def use_persistent(self, enable: bool):
+        """One persistent launch per step (default) or one launch per phase."""
+        call("natrix_batch_set_persistent", self.handle, 1 if enable else 0)
+        self.persistent = bool(enable)
 
     def add_velocity(self, sim, position, velocity, radius):
         call("natrix_batch_add_velocity", self.handle, int(sim), position[0], position[1],
@@ -166,7 +172,9 @@ class FluidBatch:
         name = torch.cuda.get_device_name()
         hist = np.bincount([size_class(w, h) for w, h in zip(self.widths, self.heights)],
                            minlength=3)
-        return f"{name}|classes={hist.tolist()}|cells={sum(w * h for w, h in zip(self.widths, self.heights))}"
+        mode = "persistent" if getattr(self, "persistent", True) else "per-phase"
+        return (f"{name}|{mode}|classes={hist.tolist()}"
+                f"|cells={sum(w * h for w, h in zip(self.widths, self.heights))}")
 
     def destroy(self):
         if self._handle:

@@ -22,10 +22,12 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/natrix.h"
 #include "cells.cuh"
+#include "jacobi_tile.cuh"
 
 using namespace natrix;
 
@@ -54,7 +56,10 @@ struct BatchSimDesc {
 struct StepHeader {
     float dt;
     int n_sims;
-    int pad[2];
+    int rho_cur;  // density buffer holding the state (persistent step kernel)
+    int pad;
+    unsigned long long epoch;  // steps since the work list was built
+    unsigned long long pad2;
 };
 
 // item = {sim, block x origin, block y origin, 0}
@@ -122,6 +127,526 @@ __global__ void __launch_bounds__(BX* BY)
                         it.y + threadIdx.x, it.z + threadIdx.y);
 }
 
+// ----------------------------------------------------------------------------
+// Persistent step kernel: the whole batch step in one launch.
+//
+// The host lays the step out as a list of work items in dependency order:
+// for every phase (forcing, advection, vorticity, viscosity, divergence,
+// Jacobi chunks 1..M, gradient subtraction, density advection), every
+// simulation's items of that phase (bands of rows for the per-cell phases,
+// tiles for the sweeps).  Resident CTAs claim items in list order from a
+// global counter (the next claim is issued while the current item runs).  An
+// item first waits until every item of its simulation's previous phase has
+// finished (a per-(simulation, phase) completion counter), runs the same
+// arithmetic as the per-phase kernels, then counts itself done.  Dependencies
+// only point to earlier items, so the earliest unfinished item can always
+// run and the kernel cannot deadlock, whatever the number of resident CTAs.
+//
+// Counters never reset: the claim counter and the completion counters grow by
+// a fixed amount per step, and the step's epoch (in the step block) gives the
+// targets.  A wait that runs out (about a second) sets status bit 2 and the
+// item runs anyway, so the launch always ends.
+//
+// Fields written earlier in the launch by other CTAs are read through L2
+// (CG loads, coherent across SMs); the sweep tiles read them by TMA after a
+// proxy fence.
+enum StepItemKind : int {
+    ITEM_FORCE = 0,
+    ITEM_ADVECT,
+    ITEM_CALC_VORT,
+    ITEM_APPLY_VORT,
+    ITEM_VISC,
+    ITEM_DIV,
+    ITEM_JACOBI,  // tile configuration in `config`
+    ITEM_SUBGRAD,
+    ITEM_DENSITY
+};
+
+struct StepItem {
+    int kind;
+    int sim;
+    int a, b;    // per-cell items: rows [a, b); Jacobi: tile origin (a, b)
+    int src;     // Jacobi: source pressure buffer
+    int sweeps;  // Jacobi: sweeps of this chunk
+    int config;  // Jacobi: tile configuration
+    int wait;    // completion counter to wait on (-1: none)
+    int need;    // items that counter gains per step
+    int done;    // completion counter this item increments
+    int pad[2];
+};
+
+constexpr int kStepThreadsY = 16;  // CTA of 32 x 16 threads (16 warps)
+using TbStep = TbCfg<64, 32, 8, kStepThreadsY>;  // Tb's tile on 512 threads
+static_assert(RtB::THREADS == 32 * kStepThreadsY && RtA::THREADS == 32 * kStepThreadsY,
+              "register tiles run with the step kernel's 512 threads");
+
+struct StepArgs {
+    const StepItem* items;
+    int n_items;
+    int n_sims;
+    const BatchSimDesc* desc;
+    const JacobiBatchSim* jsims;
+    unsigned long long* counters;
+    unsigned long long* claim;
+    const unsigned char* step;  // step block: header, op / shape ranges, ops, shapes
+    size_t ops_off, shapes_off;
+    int* status;
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Bounded wait (about 2^24 polls with back-off) for *c >= target.
+__device__ __forceinline__ bool wait_counter(const unsigned long long* c,
+                                             unsigned long long target) {
+    for (int it = 0; it < (1 << 24); ++it) {
+        if (ld_acquire_u64(c) >= target) return true;
+        __nanosleep(64);
+    }
+    return false;
+}
+
+// Order generic-proxy writes (other CTAs' stores released through a
+// completion counter; this CTA's use of the staging memory) before the
+// async-proxy copies the calling thread issues next.
+__device__ __forceinline__ void fence_before_tma() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    fence_proxy_async();
+}
+
+// A register tile of the step kernel.  `issued`: its copies were already
+// issued (prefetched during the previous item).  Once the tile sits in
+// registers, `prefetch()` may issue the next item's copies into the freed
+// staging buffers.
+template <class C, class Prefetch>
+__device__ __forceinline__ void step_rt_tile(const TileJob& job, unsigned char* smem,
+                                             uint64_t* bar, uint32_t parity, int* status,
+                                             int tid, bool issued, Prefetch prefetch) {
+    __shared__ int s_ok;
+    if (tid == 0) {
+        if (!issued) {
+            fence_before_tma();
+            issue_tile_loads<C>(smem, bar, job);
+        }
+        bool ok = wait_phase(bar, parity);
+        if (!ok) {
+            atomicOr(status, 1);
+            wait_phase(bar, parity);
+        }
+        s_ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_ok) rt_tile_body<C>(job, smem, prefetch);
+}
+
+__device__ __forceinline__ void step_tb_tile(const TileJob& job, unsigned char* smem,
+                                             uint64_t* bar, uint32_t parity, int* status,
+                                             int tid) {
+    using C = TbStep;
+    __shared__ int s_ok;
+    if (tid == 0) {
+        fence_before_tma();
+        mbar_expect_tx(bar, 2 * C::P_BYTES + C::F_BYTES);
+        tma_load_2d(smem + C::OFF_A, job.p, job.tile_x - C::HXP, job.tile_y - C::HALO, bar);
+        tma_load_2d(smem + C::OFF_D, job.d, job.tile_x - C::HXP, job.tile_y - C::HALO, bar);
+        tma_load_2d(smem + C::OFF_F, job.f, job.tile_x - C::HXF, job.tile_y - C::HALO, bar);
+        bool ok = wait_phase(bar, parity);
+        if (!ok) {
+            atomicOr(status, 1);
+            wait_phase(bar, parity);
+        }
+        s_ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_ok) tb_tile_body<C>(job, smem);
+}
+
+// Per-cell phases of the step kernel, K cells per thread: (x, y + 16 j),
+// j < K.  Every load of the K cells is issued before any of their
+// arithmetic (unconditional, in-bounds loads whose values the arithmetic may
+// not use), so one CTA of 16 warps keeps several L2 requests in flight per
+// thread; the arithmetic is the cell bodies' own helpers (cells.cuh), so the
+// values are the same.  Offsets are 32-bit: natrix_batch_create takes sides
+// of at most 32768 cells, so a simulation's offsets stay below 2^30.
+constexpr int kCellsPerThread = 2;
+
+// Clamped neighbour offsets of cell (x, y) (common.sh:9-19).
+struct Nbr32 {
+    int c, l, r, b, t;
+};
+__device__ __forceinline__ Nbr32 nbrs32(const Grid& g, int x, int y) {
+    Nbr32 n;
+    n.c = y * g.P + x;
+    n.l = x > 0 ? n.c - 1 : n.c;
+    n.r = x < g.W - 1 ? n.c + 1 : n.c;
+    n.b = y > 0 ? n.c - g.P : n.c;
+    n.t = y < g.H - 1 ? n.c + g.P : n.c;
+    return n;
+}
+
+// vel_at with a 32-bit offset and an L2 load.
+__device__ __forceinline__ float2 vel_at32(const float2* v, const Grid& g, int x, int y,
+                                           bool zb) {
+    if (zb && (x == 0 || x == g.W - 1 || y == 0 || y == g.H - 1)) return make_float2(0.0f, 0.0f);
+    return __ldcg(v + y * g.P + x);
+}
+
+__device__ __noinline__ void band_advect(const BatchSimDesc* sd, const StepParams sp, int a,
+                                         int b) {
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const Grid g = sd->g;
+    const bool zb = sp.has_borders != 0;
+    const float2* vin = sd->vel[0];
+    float2* vout = sd->vel[1];
+    const uint8_t* mask = sd->mask;
+    for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
+        for (int x = tx; x < g.W; x += BX) {
+            bool act[kCellsPerThread], obs[kCellsPerThread];
+            float2 vc[kCellsPerThread];
+#pragma unroll
+            for (int j = 0; j < kCellsPerThread; ++j) {
+                const int y = y0 + j * kStepThreadsY;
+                act[j] = y < b;
+                obs[j] = act[j] && !sp.mask_zero && __ldcg(mask + y * g.P + x);
+                vc[j] = act[j] ? vel_at32(vin, g, x, y, zb) : make_float2(0.0f, 0.0f);
+            }
+            float2 q[kCellsPerThread][4];
+            Corners c[kCellsPerThread];
+#pragma unroll
+            for (int j = 0; j < kCellsPerThread; ++j) {
+                const int y = y0 + j * kStepThreadsY;
+                c[j] = advect_corners(vc[j], x, y, g, &sp);
+                if (act[j]) {
+                    q[j][0] = vel_at32(vin, g, c[j].lo_x, c[j].hi_y, zb);
+                    q[j][1] = vel_at32(vin, g, c[j].hi_x, c[j].hi_y, zb);
+                    q[j][2] = vel_at32(vin, g, c[j].lo_x, c[j].lo_y, zb);
+                    q[j][3] = vel_at32(vin, g, c[j].hi_x, c[j].lo_y, zb);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kCellsPerThread; ++j) {
+                const int y = y0 + j * kStepThreadsY;
+                if (!act[j]) continue;
+                vout[y * g.P + x] =
+                    obs[j] ? make_float2(0.0f, 0.0f)
+                           : advect_mix(q[j][0], q[j][1], q[j][2], q[j][3], c[j], sp.dissipation);
+            }
+        }
+}
+
+__device__ __noinline__ void band_divergence(const BatchSimDesc* sd, const StepParams sp, int a,
+                                             int b) {
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const Grid g = sd->g;
+    const float2* v = sd->vel[sd->last];
+    const uint8_t* mask = sd->mask;
+    const bool mz = sp.mask_zero != 0;
+    for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
+        for (int x = tx; x < g.W; x += BX) {
+            uint32_t m[kCellsPerThread];  // obstacle bits of l, r, b, t
+            float t[kCellsPerThread][4];
+#pragma unroll
+            for (int j = 0; j < kCellsPerThread; ++j) {
+                const int y = y0 + j * kStepThreadsY;
+                if (y >= b) continue;
+                const Nbr32 n = nbrs32(g, x, y);
+                m[j] = mz ? 0u
+                          : (__ldcg(mask + n.l) ? 1u : 0u) | (__ldcg(mask + n.r) ? 2u : 0u) |
+                                (__ldcg(mask + n.b) ? 4u : 0u) | (__ldcg(mask + n.t) ? 8u : 0u);
+                t[j][0] = __ldcg(v + n.l).x;
+                t[j][1] = __ldcg(v + n.r).x;
+                t[j][2] = __ldcg(v + n.b).y;
+                t[j][3] = __ldcg(v + n.t).y;
+            }
+#pragma unroll
+            for (int j = 0; j < kCellsPerThread; ++j) {
+                const int y = y0 + j * kStepThreadsY;
+                if (y >= b) continue;
+                const int c = y * g.P + x;
+                const bool ol = m[j] & 1u, orr = m[j] & 2u, ob = m[j] & 4u, ot = m[j] & 8u;
+                const float bv = divergence_of(ol ? 0.0f : t[j][0], orr ? 0.0f : t[j][1],
+                                               ob ? 0.0f : t[j][2], ot ? 0.0f : t[j][3]);
+                sd->div[c] = bv;
+                sd->flags[c] = nb_flags(x, y, g, ol, orr, ob, ot);
+                sd->p[0][c] = (0.0f - bv) * 0.25f;
+            }
+        }
+}
+
+__device__ __noinline__ void band_subgrad(const BatchSimDesc* sd, int a, int b) {
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const Grid g = sd->g;
+    const float* p = sd->p[sd->p_final];
+    const float2* vin = sd->vel[sd->last];
+    const uint8_t* flags = sd->flags;
+    float2* vout = sd->vel[0];
+    for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
+        for (int x = tx; x < g.W; x += BX) {
+            uint8_t f[kCellsPerThread];
+            float pv[kCellsPerThread][5];
+            float2 vc[kCellsPerThread];
+#pragma unroll
+            for (int j = 0; j < kCellsPerThread; ++j) {
+                const int y = y0 + j * kStepThreadsY;
+                if (y >= b) continue;
+                const Nbr32 n = nbrs32(g, x, y);
+                f[j] = __ldcg(flags + n.c);
+                pv[j][0] = __ldcg(p + n.c);
+                pv[j][1] = __ldcg(p + n.l);
+                pv[j][2] = __ldcg(p + n.r);
+                pv[j][3] = __ldcg(p + n.b);
+                pv[j][4] = __ldcg(p + n.t);
+                vc[j] = __ldcg(vin + n.c);
+            }
+#pragma unroll
+            for (int j = 0; j < kCellsPerThread; ++j) {
+                const int y = y0 + j * kStepThreadsY;
+                if (y >= b) continue;
+                vout[y * g.P + x] = subtract_gradient_of(vc[j], f[j], pv[j][0], pv[j][1],
+                                                         pv[j][2], pv[j][3], pv[j][4]);
+            }
+        }
+}
+
+// Density advection on a density grid of the velocity grid's size (the batch
+// keeps them equal); the obstacles are reset before it runs.
+__device__ __noinline__ void band_density(const BatchSimDesc* sd, const StepParams sp, int rc,
+                                          int a, int b) {
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const Grid g = sd->g;
+    const float* rin = sd->rho[rc];
+    float* rout = sd->rho[1 - rc];
+    const float2* v = sd->vel[0];
+    for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
+        for (int x = tx; x < g.W; x += BX) {
+            float2 u[kCellsPerThread];
+#pragma unroll
+            for (int j = 0; j < kCellsPerThread; ++j) {
+                const int y = y0 + j * kStepThreadsY;
+                if (y >= b) continue;
+                const Corners cv = density_vel_corners(x, y, g, g);
+                const float2 q0 = __ldcg(v + cv.hi_y * g.P + cv.lo_x);
+                const float2 q1 = __ldcg(v + cv.hi_y * g.P + cv.hi_x);
+                const float2 q2 = __ldcg(v + cv.lo_y * g.P + cv.lo_x);
+                const float2 q3 = __ldcg(v + cv.lo_y * g.P + cv.hi_x);
+                if (on_centre(cv)) {
+                    u[j] = q2;
+                } else {  // sample_vel's arithmetic
+                    const float h1x = mixf(q0.x, q1.x, cv.dx), h1y = mixf(q0.y, q1.y, cv.dx);
+                    const float h2x = mixf(q2.x, q3.x, cv.dx), h2y = mixf(q2.y, q3.y, cv.dx);
+                    u[j] = make_float2(mixf(h2x, h1x, cv.dy), mixf(h2y, h1y, cv.dy));
+                }
+            }
+            float r[kCellsPerThread][4];
+            Corners c[kCellsPerThread];
+#pragma unroll
+            for (int j = 0; j < kCellsPerThread; ++j) {
+                const int y = y0 + j * kStepThreadsY;
+                if (y >= b) continue;
+                c[j] = density_corners(u[j], x, y, g, g, &sp);
+                r[j][0] = __ldcg(rin + c[j].hi_y * g.P + c[j].lo_x);
+                r[j][1] = __ldcg(rin + c[j].hi_y * g.P + c[j].hi_x);
+                r[j][2] = __ldcg(rin + c[j].lo_y * g.P + c[j].lo_x);
+                r[j][3] = __ldcg(rin + c[j].lo_y * g.P + c[j].hi_x);
+            }
+#pragma unroll
+            for (int j = 0; j < kCellsPerThread; ++j) {
+                const int y = y0 + j * kStepThreadsY;
+                if (y >= b) continue;
+                // sample_scalar's arithmetic
+                const float h1 = mixf(r[j][0], r[j][1], c[j].dx);
+                const float h2 = mixf(r[j][2], r[j][3], c[j].dx);
+                rout[y * g.P + x] = mixf(h2, h1, c[j].dy) * sp.d_dissipation;
+            }
+        }
+}
+
+// Cells of rows [a, b), one cell per thread at a time (vorticity and
+// viscosity items).
+template <class F>
+__device__ __forceinline__ void band_cells(int a, int b, int W, F f) {
+    for (int y = a + (int)threadIdx.y; y < b; y += kStepThreadsY)
+        for (int x = threadIdx.x; x < W; x += BX) f(x, y);
+}
+
+// Per-step values of the step block, kept in shared memory so no register
+// holds them across the items.
+struct StepShared {
+    unsigned long long epoch, base;
+    const int* op_begin;
+    const int* op_count;
+    const int* sh_begin;
+    const int* sh_count;
+    const ForceOp* ops;
+    const ShapeOp* shapes;
+    float dt;
+    int rc;
+};
+
+__device__ __forceinline__ StepParams step_params(const BatchSimDesc* sd, const StepShared& ss,
+                                                  int sim) {
+    StepParams sp = sd->sp;
+    sp.dt = ss.dt;
+    // obstacles are reset every step: no shapes this step, empty mask
+    sp.mask_zero = ss.sh_count[sim] == 0 ? 1 : 0;
+    return sp;
+}
+
+__global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const StepArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ int s_item, s_pref;
+    __shared__ StepShared ss;
+    const int tid = threadIdx.x + 32 * threadIdx.y;
+    if (tid == 0) {
+        const StepHeader* hdr = reinterpret_cast<const StepHeader*>(a.step);
+        ss.epoch = hdr->epoch;
+        ss.rc = hdr->rho_cur;
+        ss.dt = hdr->dt;
+        ss.op_begin = reinterpret_cast<const int*>(a.step + sizeof(StepHeader));
+        ss.op_count = ss.op_begin + a.n_sims;
+        ss.sh_begin = ss.op_count + a.n_sims;
+        ss.sh_count = ss.sh_begin + a.n_sims;
+        ss.ops = reinterpret_cast<const ForceOp*>(a.step + a.ops_off);
+        ss.shapes = reinterpret_cast<const ShapeOp*>(a.step + a.shapes_off);
+        // every CTA claims until it draws an index past the list: n_items +
+        // gridDim.x claims per step
+        ss.base = ss.epoch * (unsigned long long)(a.n_items + gridDim.x);
+        mbar_init(&s_bar, 1);
+        fence_barrier_init();
+        s_item = (int)(atomicAdd(a.claim, 1ull) - ss.base);
+        s_pref = 0;
+    }
+    __syncthreads();
+    uint32_t parity = 0;
+    for (;;) {
+        const int k = s_item;
+        if (k >= a.n_items) break;
+        const bool issued = s_pref != 0;
+        unsigned long long next = 0;
+        if (tid == 0) next = atomicAdd(a.claim, 1ull);  // in flight during the item
+        const StepItem it = a.items[k];
+        if (tid == 0 && it.wait >= 0 &&
+            !wait_counter(a.counters + it.wait, (ss.epoch + 1) * (unsigned long long)it.need))
+            atomicOr(a.status, 2);
+        __syncthreads();  // s_item, s_pref read by all; dependency satisfied
+        if (tid == 0) s_pref = 0;
+        const BatchSimDesc* sd = a.desc + it.sim;
+        switch (it.kind) {
+            case ITEM_FORCE: {
+                const int ns = ss.sh_count[it.sim], no = ss.op_count[it.sim];
+                const Grid g = sd->g;
+                constexpr int kRows = 4 * kStepThreadsY;  // rows per block call
+                for (int by = it.a; by < it.b; by += kRows)
+                    for (int bx = 0; bx < g.W; bx += BX) {
+                        if (ns)
+                            block_obstacles<4, kStepThreadsY>(
+                                sd->mask, g, ss.shapes + ss.sh_begin[it.sim], ns, 1, bx, by);
+                        if (no)
+                            block_forcing<4, kStepThreadsY, true>(
+                                sd->vel[0], g, sd->rho[ss.rc], g, ss.ops + ss.op_begin[it.sim],
+                                no, bx, by);
+                    }
+                break;
+            }
+            case ITEM_ADVECT:
+                band_advect(sd, step_params(sd, ss, it.sim), it.a, it.b);
+                break;
+            case ITEM_CALC_VORT: {
+                const Grid g = sd->g;
+                band_cells(it.a, it.b, g.W, [&](int x, int y) {
+                    cell_calc_vorticity<true>(sd->vel[sd->vort_in], sd->vort, g, x, y);
+                });
+                break;
+            }
+            case ITEM_APPLY_VORT: {
+                const Grid g = sd->g;
+                const StepParams sp = step_params(sd, ss, it.sim);
+                band_cells(it.a, it.b, g.W, [&](int x, int y) {
+                    cell_apply_vorticity<true>(sd->vel[sd->vort_in], sd->vel[sd->vort_out],
+                                               sd->vort, g, &sp, x, y);
+                });
+                break;
+            }
+            case ITEM_VISC: {
+                const Grid g = sd->g;
+                const StepParams sp = step_params(sd, ss, it.sim);
+                band_cells(it.a, it.b, g.W, [&](int x, int y) {
+                    cell_viscosity<true>(sd->vel[sd->visc_in], sd->vel[sd->visc_out], g, &sp, x,
+                                         y);
+                });
+                break;
+            }
+            case ITEM_DIV:
+                band_divergence(sd, step_params(sd, ss, it.sim), it.a, it.b);
+                break;
+            case ITEM_JACOBI: {
+                const JacobiBatchSim& js = a.jsims[it.sim];
+                const TileJob job{&js.maps.p[it.src], &js.maps.div, &js.maps.flags,
+                                  js.p[1 - it.src], js.g, it.sweeps, it.a, it.b, nullptr, nullptr};
+                // prefetch: when the next claimed item is a tile of the same
+                // configuration whose dependency is already complete, issue
+                // its copies as soon as this tile sits in registers
+                auto prefetch = [&](auto* tag) {
+                    using C = std::remove_pointer_t<decltype(tag)>;
+                    if (tid != 0) return;
+                    const long long nk = (long long)(next - ss.base);
+                    if (nk >= a.n_items) return;
+                    const StepItem nx = a.items[nk];
+                    if (nx.kind != ITEM_JACOBI || nx.config != it.config) return;
+                    if (nx.wait >= 0 && ld_acquire_u64(a.counters + nx.wait) <
+                                            (ss.epoch + 1) * (unsigned long long)nx.need)
+                        return;
+                    const JacobiBatchSim& ns = a.jsims[nx.sim];
+                    const TileJob nj{&ns.maps.p[nx.src], &ns.maps.div, &ns.maps.flags,
+                                     ns.p[1 - nx.src], ns.g, nx.sweeps, nx.a, nx.b, nullptr,
+                                     nullptr};
+                    fence_before_tma();
+                    issue_tile_loads<C>(smem, &s_bar, nj);
+                    s_pref = 1;
+                };
+                if (it.config == JACOBI_RT_B)
+                    step_rt_tile<RtB>(job, smem, &s_bar, parity, a.status, tid, issued,
+                                      [&] { prefetch((RtB*)nullptr); });
+                else if (it.config == JACOBI_RT_A)
+                    step_rt_tile<RtA>(job, smem, &s_bar, parity, a.status, tid, issued,
+                                      [&] { prefetch((RtA*)nullptr); });
+                else
+                    step_tb_tile(job, smem, &s_bar, parity, a.status, tid);
+                parity ^= 1u;
+                break;
+            }
+            case ITEM_SUBGRAD:
+                band_subgrad(sd, it.a, it.b);
+                break;
+            case ITEM_DENSITY: {
+                // the fluid update resets the obstacles before the density
+                // update runs (natrix/core/fluid_simulator.py:267-280)
+                StepParams sp = step_params(sd, ss, it.sim);
+                sp.mask_zero = 1;
+                band_density(sd, sp, ss.rc, it.a, it.b);
+                break;
+            }
+            default: break;
+        }
+        __syncthreads();  // the item's writes are done
+        if (tid == 0) {
+            __threadfence();
+            atomicAdd(a.counters + it.done, 1ull);
+            s_item = (int)(next - ss.base);
+        }
+        __syncthreads();
+    }
+}
+
+constexpr int step_smem_bytes() {
+    return RtB::SMEM > RtA::SMEM ? (RtB::SMEM > TbStep::SMEM ? RtB::SMEM : TbStep::SMEM)
+                                 : (RtA::SMEM > TbStep::SMEM ? RtA::SMEM : TbStep::SMEM);
+}
+
 int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
 int fail(int code, const char* msg) { return set_last_error(code, msg); }
@@ -185,9 +710,147 @@ struct natrix_batch {
     int* d_status = nullptr;
     int64_t launches = 0;
     int launches_per_step = 0;
+    // persistent step kernel (one launch per step) or one launch per phase
+    bool persistent = true;
+    StepItem* d_items = nullptr;
+    size_t items_cap = 0;
+    int n_items = 0;
+    unsigned long long* d_counters = nullptr;  // [n_sims][phases] completions
+    size_t counters_cap = 0;
+    unsigned long long* d_claim = nullptr;
+    unsigned long long epoch = 0;
+    int step_grid = 0;
 };
 
 namespace {
+
+// The persistent kernel's work list: phases in order, within a phase the
+// simulations by decreasing sweep work (the longest dependency chains start
+// first), per simulation its bands of rows (per-cell phases: about 16k
+// cells, a multiple of 64 rows) or its sweep tiles.  Each item waits for all
+// items of its simulation's previous phase.
+int build_step_items(natrix_batch* b, const std::vector<int>& cfg_of,
+                     const std::vector<int>& per_of, const std::vector<int>& launches_of,
+                     int max_launches) {
+    const int n = b->n;
+    const int kF = 0, kA = 1, kCV = 2, kAV = 3, kVS = 4, kD = 5, kJ = 6;
+    const int kS = kJ + max_launches, kR = kS + 1, phases = kR + 1;
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        const double wx = (double)b->grids[x].W * b->grids[x].H * b->prm[x].iterations;
+        const double wy = (double)b->grids[y].W * b->grids[y].H * b->prm[y].iterations;
+        return wx > wy;
+    });
+    // bands of a multiple of 64 rows (the forcing item's block height)
+    auto band_rows = [](const Grid& g) {
+        const int r = (16384 / g.W) / 64 * 64;
+        return r < 64 ? 64 : r;
+    };
+    auto bands = [&](const Grid& g) { return (g.H + band_rows(g) - 1) / band_rows(g); };
+    auto tiles = [&](int i) {
+        int tx, ty;
+        jacobi_tile(cfg_of[i], &tx, &ty);
+        const Grid& g = b->grids[i];
+        return ((g.W + tx - 1) / tx) * ((g.H + ty - 1) / ty);
+    };
+    // the phases each simulation runs, in order
+    std::vector<std::vector<int>> seq(n);
+    for (int i = 0; i < n; ++i) {
+        seq[i].push_back(kF);
+        seq[i].push_back(kA);
+        if (b->prm[i].vorticity > 0.0f) {
+            seq[i].push_back(kCV);
+            seq[i].push_back(kAV);
+        }
+        if (b->prm[i].viscosity > 0.0f) seq[i].push_back(kVS);
+        seq[i].push_back(kD);
+        for (int m = 0; m < launches_of[i]; ++m) seq[i].push_back(kJ + m);
+        seq[i].push_back(kS);
+        seq[i].push_back(kR);
+    }
+    auto count_of = [&](int i, int ph) {
+        return (ph >= kJ && ph < kS) ? tiles(i) : bands(b->grids[i]);
+    };
+    std::vector<StepItem> items;
+    for (int ph = 0; ph < phases; ++ph) {
+        for (int i : order) {
+            const auto& q = seq[i];
+            const auto pos = std::find(q.begin(), q.end(), ph);
+            if (pos == q.end()) continue;
+            StepItem base{};
+            base.sim = i;
+            base.done = i * phases + ph;
+            if (pos == q.begin()) {
+                base.wait = -1;
+            } else {
+                const int prev = *(pos - 1);
+                base.wait = i * phases + prev;
+                base.need = count_of(i, prev);
+            }
+            const Grid& g = b->grids[i];
+            if (ph >= kJ && ph < kS) {
+                const int m = ph - kJ;
+                int tx, ty;
+                jacobi_tile(cfg_of[i], &tx, &ty);
+                base.kind = ITEM_JACOBI;
+                base.config = cfg_of[i];
+                base.src = m & 1;
+                base.sweeps = std::min(b->prm[i].iterations - 1 - m * per_of[i], per_of[i]);
+                for (int y = 0; y < g.H; y += ty)
+                    for (int x = 0; x < g.W; x += tx) {
+                        StepItem t = base;
+                        t.a = x;
+                        t.b = y;
+                        items.push_back(t);
+                    }
+                continue;
+            }
+            base.kind = ph == kF    ? ITEM_FORCE
+                        : ph == kA  ? ITEM_ADVECT
+                        : ph == kCV ? ITEM_CALC_VORT
+                        : ph == kAV ? ITEM_APPLY_VORT
+                        : ph == kVS ? ITEM_VISC
+                        : ph == kD  ? ITEM_DIV
+                        : ph == kS  ? ITEM_SUBGRAD
+                                    : ITEM_DENSITY;
+            const int rows = band_rows(g);
+            for (int y = 0; y < g.H; y += rows) {
+                StepItem t = base;
+                t.a = y;
+                t.b = std::min(y + rows, g.H);
+                items.push_back(t);
+            }
+        }
+    }
+    cudaError_t e = upload_vec(&b->d_items, &b->items_cap, items);
+    b->n_items = (int)items.size();
+    const size_t nc = (size_t)n * phases;
+    if (e == cudaSuccess && b->counters_cap < nc) {
+        cudaFree(b->d_counters);
+        b->d_counters = nullptr;
+        e = cudaMalloc(&b->d_counters, nc * sizeof(unsigned long long));
+        if (e == cudaSuccess) b->counters_cap = nc;
+    }
+    if (e == cudaSuccess && !b->d_claim) e = cudaMalloc(&b->d_claim, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(b->d_counters, 0, nc * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(b->d_claim, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess && b->step_grid == 0) {
+        e = cudaFuncSetAttribute(k_batch_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 step_smem_bytes());
+        int per_sm = 0, sms = 0;
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_step,
+                                                              32 * kStepThreadsY,
+                                                              step_smem_bytes());
+        if (e == cudaSuccess)
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+        if (e == cudaSuccess) b->step_grid = std::max(1, per_sm) * std::max(1, sms);
+    }
+    if (e != cudaSuccess) return fail(NATRIX_ECUDA, cudaGetErrorString(e));
+    b->epoch = 0;
+    return NATRIX_OK;
+}
 
 // Rebuild descriptors, item lists and Jacobi launch lists (host -> device).
 int rebuild(natrix_batch* b) {
@@ -250,6 +913,10 @@ int rebuild(natrix_batch* b) {
         js.p[0] = b->desc[i].p[0];
         js.p[1] = b->desc[i].p[1];
         js.g = b->grids[i];
+    }
+    if (b->persistent) {
+        const int rc = build_step_items(b, cfg_of, per_of, launches_of, max_launches);
+        if (rc) return rc;
     }
     for (auto& l : b->jl) cudaFree(l.items);
     b->jl.clear();
@@ -326,6 +993,13 @@ cudaError_t enqueue_step(natrix_batch* b, int rho_cur, cudaStream_t st, int* lau
     const size_t shapes_off = ops_off + (size_t)kMaxOpsPerLaunch * n * sizeof(ForceOp);
     const ShapeOp* shapes = reinterpret_cast<const ShapeOp*>(b->d_step + shapes_off);
     int count = 0;
+    if (b->persistent) {
+        const StepArgs a{b->d_items, b->n_items, n, b->d_desc, b->d_jsims, b->d_counters,
+                         b->d_claim, b->d_step, ops_off, shapes_off, b->d_status};
+        k_batch_step<<<b->step_grid, dim3(BX, kStepThreadsY), step_smem_bytes(), st>>>(a);
+        *launches = 1;
+        return cudaGetLastError();
+    }
     k_batch_prepare<<<(n + 127) / 128, 128, 0, st>>>(b->d_desc, hdr, sh_count);
     ++count;
     const int na = b->items_all.n;
@@ -380,6 +1054,9 @@ void free_batch(natrix_batch* b) {
     cudaFree(b->d_jsims);
     cudaFree(b->d_step);
     cudaFree(b->d_status);
+    cudaFree(b->d_items);
+    cudaFree(b->d_counters);
+    cudaFree(b->d_claim);
     cudaFree(b->arena);
     if (b->h_step) cudaFreeHost(b->h_step);
     delete b;
@@ -509,6 +1186,15 @@ int natrix_batch_set_graph(natrix_batch* b, int32_t enable) {
     return NATRIX_OK;
 }
 
+int natrix_batch_set_persistent(natrix_batch* b, int32_t enable) {
+    if (!b) return fail(NATRIX_EINVAL, "NULL handle");
+    if (b->persistent != (enable != 0)) {
+        b->persistent = enable != 0;
+        b->dirty = true;
+    }
+    return NATRIX_OK;
+}
+
 int natrix_batch_add_velocity(natrix_batch* b, int32_t sim, float px, float py, float vx,
                               float vy, float radius) {
     if (!b || sim < 0 || sim >= b->n) return fail(NATRIX_EINVAL, "bad arguments");
@@ -583,7 +1269,7 @@ int natrix_batch_step(natrix_batch* b, float dt, void* stream) {
     cudaError_t e = cudaEventSynchronize(b->step_ev[slot]);
     if (e != cudaSuccess) return fail(NATRIX_ECUDA, cudaGetErrorString(e));
     unsigned char* h = b->h_step + slot * b->step_cap;
-    StepHeader hdr{dt, n, {0, 0}};
+    StepHeader hdr{dt, n, b->rho_cur, 0, b->epoch, 0};
     std::memcpy(h, &hdr, sizeof hdr);
     int* ranges = reinterpret_cast<int*>(h + sizeof(StepHeader));
     const size_t ops_off = sizeof(StepHeader) + 4 * (size_t)n * sizeof(int);
@@ -638,6 +1324,7 @@ int natrix_batch_step(natrix_batch* b, float dt, void* stream) {
     if (e != cudaSuccess) return fail(NATRIX_ECUDA, cudaGetErrorString(e));
     b->launches += launches;
     b->rho_cur ^= 1;
+    ++b->epoch;
     return NATRIX_OK;
 }
 

@@ -72,12 +72,16 @@ def compare(batch, singles):
                              s.download(_lib.FIELD_VORTICITY), f"sim {i} vorticity")
 
 
-@pytest.mark.parametrize("tuning,graph", [
-    ({0: (0, 8), 1: (1, 8), 2: (2, 8)}, True),
-    ({0: (0, 4), 1: (0, 8), 2: (1, 4)}, True),
-    ({0: (1, 8), 1: (2, 3), 2: (0, 5)}, False),
+@pytest.mark.parametrize("tuning,graph,persistent", [
+    ({0: (0, 8), 1: (1, 8), 2: (2, 8)}, True, True),
+    ({0: (0, 4), 1: (0, 8), 2: (1, 4)}, True, True),
+    ({0: (1, 8), 1: (2, 3), 2: (0, 5)}, False, True),
+    ({0: (0, 8), 1: (1, 8), 2: (2, 8)}, True, False),
+    ({0: (1, 8), 1: (2, 3), 2: (0, 5)}, False, False),
 ])
-def test_batch_equals_single_simulators(cuda, tuning, graph):
+def test_batch_equals_single_simulators(cuda, tuning, graph, persistent):
+    """Persistent: the whole step in one launch (work items in dependency
+    order); otherwise one launch per phase."""
     rng = np.random.default_rng(1)
     n = len(SIDES)
     iters = [int(x) for x in rng.choice([1, 9, 20, 40, 80], n)]
@@ -85,12 +89,15 @@ def test_batch_equals_single_simulators(cuda, tuning, graph):
     nus = [0.1 if i % 4 == 1 else 0.0 for i in range(n)]
     batch, singles = build(iters, eps, nus, 2)
     batch.use_graph(graph)
+    batch.use_persistent(persistent)
     for c, (cfg, spl) in tuning.items():
         batch.set_tuning(c, cfg, spl)
     drive(batch, singles, steps=5, seed=3)
     compare(batch, singles)
     total, per_step = batch.launches()
     assert per_step > 0 and total >= 5 * per_step
+    if persistent:
+        assert per_step == 1
     batch.destroy()
     for s, d in singles:
         d.destroy()
