@@ -267,11 +267,13 @@ __device__ __forceinline__ void step_tb_tile(const TileJob& job, unsigned char* 
 // Per-cell phases of the step kernel, K cells per thread: (x, y + 16 j),
 // j < K.  Every load of the K cells is issued before any of their
 // arithmetic (unconditional, in-bounds loads whose values the arithmetic may
-// not use), so one CTA of 16 warps keeps several L2 requests in flight per
-// thread; the arithmetic is the cell bodies' own helpers (cells.cuh), so the
-// values are the same.  Offsets are 32-bit: natrix_batch_create takes sides
+// not use), so each cell costs one round of L2 requests; the arithmetic is
+// the cell bodies' own helpers (cells.cuh), so the values are the same.
+// K = 1: with more cells in flight the kernel, capped at 128 registers by
+// the sweep tile, spills into the tile's sweep loop (measured: the sweep
+// items took twice as long).  Offsets are 32-bit: natrix_batch_create takes sides
 // of at most 32768 cells, so a simulation's offsets stay below 2^30.
-constexpr int kCellsPerThread = 2;
+constexpr int kCellsPerThread = 1;
 
 // Clamped neighbour offsets of cell (x, y) (common.sh:9-19).
 struct Nbr32 {
@@ -294,15 +296,23 @@ __device__ __forceinline__ float2 vel_at32(const float2* v, const Grid& g, int x
     return __ldcg(v + y * g.P + x);
 }
 
-__device__ __noinline__ void band_advect(const BatchSimDesc* sd, const StepParams sp, int a,
+__device__ __forceinline__ void band_advect(const BatchSimDesc* sd, float dt, int mask_zero, int a,
                                          int b) {
     const int tx = threadIdx.x, ty = threadIdx.y;
     const Grid g = sd->g;
-    const bool zb = sp.has_borders != 0;
+    // the step scalars in registers (advect_corners reads dt and speed)
+    StepParams sp{};
+    sp.dt = dt;
+    sp.speed = sd->sp.speed;
+    sp.dissipation = sd->sp.dissipation;
+    sp.mask_zero = mask_zero;
+    const bool zb = sd->sp.has_borders != 0;
     const float2* vin = sd->vel[0];
     float2* vout = sd->vel[1];
     const uint8_t* mask = sd->mask;
+#pragma unroll 1
     for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
+#pragma unroll 1
         for (int x = tx; x < g.W; x += BX) {
             bool act[kCellsPerThread], obs[kCellsPerThread];
             float2 vc[kCellsPerThread];
@@ -337,14 +347,16 @@ __device__ __noinline__ void band_advect(const BatchSimDesc* sd, const StepParam
         }
 }
 
-__device__ __noinline__ void band_divergence(const BatchSimDesc* sd, const StepParams sp, int a,
+__device__ __forceinline__ void band_divergence(const BatchSimDesc* sd, int mask_zero, int a,
                                              int b) {
     const int tx = threadIdx.x, ty = threadIdx.y;
     const Grid g = sd->g;
     const float2* v = sd->vel[sd->last];
     const uint8_t* mask = sd->mask;
-    const bool mz = sp.mask_zero != 0;
+    const bool mz = mask_zero != 0;
+#pragma unroll 1
     for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
+#pragma unroll 1
         for (int x = tx; x < g.W; x += BX) {
             uint32_t m[kCellsPerThread];  // obstacle bits of l, r, b, t
             float t[kCellsPerThread][4];
@@ -376,14 +388,16 @@ __device__ __noinline__ void band_divergence(const BatchSimDesc* sd, const StepP
         }
 }
 
-__device__ __noinline__ void band_subgrad(const BatchSimDesc* sd, int a, int b) {
+__device__ __forceinline__ void band_subgrad(const BatchSimDesc* sd, int a, int b) {
     const int tx = threadIdx.x, ty = threadIdx.y;
     const Grid g = sd->g;
     const float* p = sd->p[sd->p_final];
     const float2* vin = sd->vel[sd->last];
     const uint8_t* flags = sd->flags;
     float2* vout = sd->vel[0];
+#pragma unroll 1
     for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
+#pragma unroll 1
         for (int x = tx; x < g.W; x += BX) {
             uint8_t f[kCellsPerThread];
             float pv[kCellsPerThread][5];
@@ -413,14 +427,21 @@ __device__ __noinline__ void band_subgrad(const BatchSimDesc* sd, int a, int b) 
 
 // Density advection on a density grid of the velocity grid's size (the batch
 // keeps them equal); the obstacles are reset before it runs.
-__device__ __noinline__ void band_density(const BatchSimDesc* sd, const StepParams sp, int rc,
-                                          int a, int b) {
+__device__ __forceinline__ void band_density(const BatchSimDesc* sd, float dt, int rc, int a,
+                                          int b) {
     const int tx = threadIdx.x, ty = threadIdx.y;
     const Grid g = sd->g;
+    // the step scalars in registers (density_corners reads dt and the speed)
+    StepParams sp{};
+    sp.dt = dt;
+    sp.d_speed = sd->sp.d_speed;
+    sp.d_dissipation = sd->sp.d_dissipation;
     const float* rin = sd->rho[rc];
     float* rout = sd->rho[1 - rc];
     const float2* v = sd->vel[0];
+#pragma unroll 1
     for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
+#pragma unroll 1
         for (int x = tx; x < g.W; x += BX) {
             float2 u[kCellsPerThread];
 #pragma unroll
@@ -472,6 +493,66 @@ __device__ __forceinline__ void band_cells(int a, int b, int W, F f) {
         for (int x = threadIdx.x; x < W; x += BX) f(x, y);
 }
 
+// A register-tile sweep item, item k of the list.  Thread 0 keeps the
+// tile barrier's parity and the prefetch flag in shared memory (nothing of
+// the item loop stays in registers across the sweep, which needs nearly all
+// of them).  nk: the item this CTA claimed next (>= n_items: none).  When
+// that next item is a tile of the same configuration whose dependency is
+// already complete, its copies are issued into the staging buffers as soon
+// as this tile sits in registers, and the flag tells the next item so.
+// epoch1: the step's epoch + 1 (completion targets are epoch1 * need).
+template <class C>
+__device__ __forceinline__ void jacobi_item(int k, long long nk, const StepItem* items,
+                                            int n_items, const JacobiBatchSim* jsims,
+                                            const unsigned long long* counters,
+                                            unsigned long long epoch1, unsigned char* smem,
+                                            uint64_t* bar, uint32_t* s_parity, int* status,
+                                            int* s_pref) {
+    const int tid = threadIdx.x + 32 * threadIdx.y;
+    const StepItem it = items[k];
+    const JacobiBatchSim& js = jsims[it.sim];
+    const TileJob job{&js.maps.p[it.src], &js.maps.div, &js.maps.flags, js.p[1 - it.src], js.g,
+                      it.sweeps, it.a, it.b, nullptr, nullptr};
+    bool issued = false;
+    uint32_t parity = 0;
+    if (tid == 0) {
+        issued = *s_pref != 0;
+        *s_pref = 0;
+        parity = *s_parity;
+        *s_parity ^= 1u;
+    }
+    step_rt_tile<C>(job, smem, bar, parity, status, tid, issued, [&] {
+        if (tid != 0 || nk >= n_items) return;
+        const StepItem nx = items[nk];
+        if (nx.kind != ITEM_JACOBI || nx.config != it.config) return;
+        if (nx.wait >= 0 &&
+            ld_acquire_u64(counters + nx.wait) < epoch1 * (unsigned long long)nx.need)
+            return;
+        const JacobiBatchSim& ns = jsims[nx.sim];
+        const TileJob nj{&ns.maps.p[nx.src], &ns.maps.div, &ns.maps.flags, ns.p[1 - nx.src],
+                         ns.g, nx.sweeps, nx.a, nx.b, nullptr, nullptr};
+        fence_before_tma();
+        issue_tile_loads<C>(smem, bar, nj);
+        *s_pref = 1;
+    });
+}
+
+__device__ __forceinline__ void jacobi_tb_item(int k, const StepItem* items,
+                                               const JacobiBatchSim* jsims, unsigned char* smem,
+                                               uint64_t* bar, uint32_t* s_parity, int* status) {
+    const int tid = threadIdx.x + 32 * threadIdx.y;
+    const StepItem it = items[k];
+    const JacobiBatchSim& js = jsims[it.sim];
+    const TileJob job{&js.maps.p[it.src], &js.maps.div, &js.maps.flags, js.p[1 - it.src], js.g,
+                      it.sweeps, it.a, it.b, nullptr, nullptr};
+    uint32_t parity = 0;
+    if (tid == 0) {
+        parity = *s_parity;
+        *s_parity ^= 1u;
+    }
+    step_tb_tile(job, smem, bar, parity, status, tid);
+}
+
 // Per-step values of the step block, kept in shared memory so no register
 // holds them across the items.
 struct StepShared {
@@ -499,6 +580,8 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ int s_item, s_pref;
+    __shared__ long long s_next;
+    __shared__ uint32_t s_parity;
     __shared__ StepShared ss;
     const int tid = threadIdx.x + 32 * threadIdx.y;
     if (tid == 0) {
@@ -519,53 +602,58 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
         fence_barrier_init();
         s_item = (int)(atomicAdd(a.claim, 1ull) - ss.base);
         s_pref = 0;
+        s_parity = 0;
     }
     __syncthreads();
-    uint32_t parity = 0;
     for (;;) {
         const int k = s_item;
         if (k >= a.n_items) break;
-        const bool issued = s_pref != 0;
         unsigned long long next = 0;
-        if (tid == 0) next = atomicAdd(a.claim, 1ull);  // in flight during the item
-        const StepItem it = a.items[k];
-        if (tid == 0 && it.wait >= 0 &&
-            !wait_counter(a.counters + it.wait, (ss.epoch + 1) * (unsigned long long)it.need))
-            atomicOr(a.status, 2);
-        __syncthreads();  // s_item, s_pref read by all; dependency satisfied
-        if (tid == 0) s_pref = 0;
-        const BatchSimDesc* sd = a.desc + it.sim;
-        switch (it.kind) {
+        if (tid == 0) next = atomicAdd(a.claim, 1ull);  // in flight during the wait
+        if (tid == 0) {
+            const StepItem w = a.items[k];
+            if (w.wait >= 0 &&
+                !wait_counter(a.counters + w.wait, (ss.epoch + 1) * (unsigned long long)w.need))
+                atomicOr(a.status, 2);
+            s_next = (long long)(next - ss.base);
+        }
+        __syncthreads();  // s_item read by all; dependency satisfied
+        const int kind = a.items[k].kind;
+        const int sim = a.items[k].sim;
+        const BatchSimDesc* sd = a.desc + sim;
+        switch (kind) {
             case ITEM_FORCE: {
-                const int ns = ss.sh_count[it.sim], no = ss.op_count[it.sim];
+                const int ra = a.items[k].a, rb = a.items[k].b;
+                const int ns = ss.sh_count[sim], no = ss.op_count[sim];
                 const Grid g = sd->g;
                 constexpr int kRows = 4 * kStepThreadsY;  // rows per block call
-                for (int by = it.a; by < it.b; by += kRows)
+                for (int by = ra; by < rb; by += kRows)
                     for (int bx = 0; bx < g.W; bx += BX) {
                         if (ns)
                             block_obstacles<4, kStepThreadsY>(
-                                sd->mask, g, ss.shapes + ss.sh_begin[it.sim], ns, 1, bx, by);
+                                sd->mask, g, ss.shapes + ss.sh_begin[sim], ns, 1, bx, by);
                         if (no)
                             block_forcing<4, kStepThreadsY, true>(
-                                sd->vel[0], g, sd->rho[ss.rc], g, ss.ops + ss.op_begin[it.sim],
-                                no, bx, by);
+                                sd->vel[0], g, sd->rho[ss.rc], g, ss.ops + ss.op_begin[sim], no,
+                                bx, by);
                     }
                 break;
             }
             case ITEM_ADVECT:
-                band_advect(sd, step_params(sd, ss, it.sim), it.a, it.b);
+                band_advect(sd, ss.dt, ss.sh_count[sim] == 0 ? 1 : 0, a.items[k].a,
+                            a.items[k].b);
                 break;
             case ITEM_CALC_VORT: {
                 const Grid g = sd->g;
-                band_cells(it.a, it.b, g.W, [&](int x, int y) {
+                band_cells(a.items[k].a, a.items[k].b, g.W, [&](int x, int y) {
                     cell_calc_vorticity<true>(sd->vel[sd->vort_in], sd->vort, g, x, y);
                 });
                 break;
             }
             case ITEM_APPLY_VORT: {
                 const Grid g = sd->g;
-                const StepParams sp = step_params(sd, ss, it.sim);
-                band_cells(it.a, it.b, g.W, [&](int x, int y) {
+                const StepParams sp = step_params(sd, ss, sim);
+                band_cells(a.items[k].a, a.items[k].b, g.W, [&](int x, int y) {
                     cell_apply_vorticity<true>(sd->vel[sd->vort_in], sd->vel[sd->vort_out],
                                                sd->vort, g, &sp, x, y);
                 });
@@ -573,70 +661,45 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
             }
             case ITEM_VISC: {
                 const Grid g = sd->g;
-                const StepParams sp = step_params(sd, ss, it.sim);
-                band_cells(it.a, it.b, g.W, [&](int x, int y) {
+                const StepParams sp = step_params(sd, ss, sim);
+                band_cells(a.items[k].a, a.items[k].b, g.W, [&](int x, int y) {
                     cell_viscosity<true>(sd->vel[sd->visc_in], sd->vel[sd->visc_out], g, &sp, x,
                                          y);
                 });
                 break;
             }
             case ITEM_DIV:
-                band_divergence(sd, step_params(sd, ss, it.sim), it.a, it.b);
+                band_divergence(sd, ss.sh_count[sim] == 0 ? 1 : 0, a.items[k].a, a.items[k].b);
                 break;
             case ITEM_JACOBI: {
-                const JacobiBatchSim& js = a.jsims[it.sim];
-                const TileJob job{&js.maps.p[it.src], &js.maps.div, &js.maps.flags,
-                                  js.p[1 - it.src], js.g, it.sweeps, it.a, it.b, nullptr, nullptr};
-                // prefetch: when the next claimed item is a tile of the same
-                // configuration whose dependency is already complete, issue
-                // its copies as soon as this tile sits in registers
-                auto prefetch = [&](auto* tag) {
-                    using C = std::remove_pointer_t<decltype(tag)>;
-                    if (tid != 0) return;
-                    const long long nk = (long long)(next - ss.base);
-                    if (nk >= a.n_items) return;
-                    const StepItem nx = a.items[nk];
-                    if (nx.kind != ITEM_JACOBI || nx.config != it.config) return;
-                    if (nx.wait >= 0 && ld_acquire_u64(a.counters + nx.wait) <
-                                            (ss.epoch + 1) * (unsigned long long)nx.need)
-                        return;
-                    const JacobiBatchSim& ns = a.jsims[nx.sim];
-                    const TileJob nj{&ns.maps.p[nx.src], &ns.maps.div, &ns.maps.flags,
-                                     ns.p[1 - nx.src], ns.g, nx.sweeps, nx.a, nx.b, nullptr,
-                                     nullptr};
-                    fence_before_tma();
-                    issue_tile_loads<C>(smem, &s_bar, nj);
-                    s_pref = 1;
-                };
-                if (it.config == JACOBI_RT_B)
-                    step_rt_tile<RtB>(job, smem, &s_bar, parity, a.status, tid, issued,
-                                      [&] { prefetch((RtB*)nullptr); });
-                else if (it.config == JACOBI_RT_A)
-                    step_rt_tile<RtA>(job, smem, &s_bar, parity, a.status, tid, issued,
-                                      [&] { prefetch((RtA*)nullptr); });
+                const int config = a.items[k].config;
+                const long long nk = s_next;
+                if (config == JACOBI_RT_B)
+                    jacobi_item<RtB>(k, nk, a.items, a.n_items, a.jsims, a.counters,
+                                     ss.epoch + 1, smem, &s_bar, &s_parity, a.status, &s_pref);
+                else if (config == JACOBI_RT_A)
+                    jacobi_item<RtA>(k, nk, a.items, a.n_items, a.jsims, a.counters,
+                                     ss.epoch + 1, smem, &s_bar, &s_parity, a.status, &s_pref);
                 else
-                    step_tb_tile(job, smem, &s_bar, parity, a.status, tid);
-                parity ^= 1u;
+                    jacobi_tb_item(k, a.items, a.jsims, smem, &s_bar, &s_parity, a.status);
                 break;
             }
             case ITEM_SUBGRAD:
-                band_subgrad(sd, it.a, it.b);
+                band_subgrad(sd, a.items[k].a, a.items[k].b);
                 break;
-            case ITEM_DENSITY: {
+            case ITEM_DENSITY:
                 // the fluid update resets the obstacles before the density
-                // update runs (natrix/core/fluid_simulator.py:267-280)
-                StepParams sp = step_params(sd, ss, it.sim);
-                sp.mask_zero = 1;
-                band_density(sd, sp, ss.rc, it.a, it.b);
+                // update runs (natrix/core/fluid_simulator.py:267-280): no
+                // mask test
+                band_density(sd, ss.dt, ss.rc, a.items[k].a, a.items[k].b);
                 break;
-            }
             default: break;
         }
         __syncthreads();  // the item's writes are done
         if (tid == 0) {
             __threadfence();
-            atomicAdd(a.counters + it.done, 1ull);
-            s_item = (int)(next - ss.base);
+            atomicAdd(a.counters + a.items[k].done, 1ull);
+            s_item = (int)s_next;
         }
         __syncthreads();
     }
@@ -711,7 +774,8 @@ struct natrix_batch {
     int64_t launches = 0;
     int launches_per_step = 0;
     // persistent step kernel (one launch per step) or one launch per phase
-    bool persistent = true;
+    // (the default: faster on the 512-simulation workload)
+    bool persistent = false;
     StepItem* d_items = nullptr;
     size_t items_cap = 0;
     int n_items = 0;
