@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(BX* BY)
 // cell's arithmetic is cell_divergence / cell_subtract_gradient's, so the
 // results are identical; these kernels need an even width (the host falls
 // back to the per-cell kernels otherwise).
-constexpr int ST_WARPS = 4, ST_COLS = 64 * ST_WARPS, ST_ROWS = 16;
+constexpr int ST_WARPS = 4, ST_COLS = 64 * ST_WARPS, ST_ROWS = 8;
 
 struct VRow {  // velocity and obstacle flag of a lane's two cells
     float2 a, b;
