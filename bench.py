@@ -804,18 +804,24 @@ def run_warmstart(args):
         sim, m = ws.evaluation_system(size, seed=7)
         regions = ws.Regions(m.view(1, size, -1), 1, size, size)
         removed = ws.project_divergence(sim, regions)
-        floor = ws.fp32_floor(sim, regions)
+        exact = ws.exact_pressure(sim, regions)
+        floor = ws.fp32_floor(sim, regions, exact)
         # 1e-4 where FP32 storage of the pressure can reach it with margin,
         # else the first of these tolerances at least 3x above the floor
         rtol = next(t for t in (1e-4, 2e-4, 5e-4, 1e-3, 2e-3, 5e-3, 1e-2) if t >= 3 * floor)
+        diag = ws.guess_diagnostics(sim, net, m, regions, exact)
         zero = ws.warm_start_solve(sim, None, m, rtol=rtol, time_limit_s=args.solve_limit,
                                    regions=regions)
         cnn = ws.warm_start_solve(sim, net, m, rtol=rtol, time_limit_s=args.solve_limit,
                                   regions=regions)
+        forced = ws.warm_start_solve(sim, net, m, rtol=rtol, time_limit_s=args.solve_limit,
+                                     regions=regions, force=True)
         sim.destroy()
         results[str(size)] = {"rtol": rtol, "fp32_floor": floor, "mean_removed": removed,
-                              "zero": zero, "network": cnn,
-                              "speedup": zero["seconds"] / max(cnn["seconds"], 1e-9)}
+                              "zero": zero, "network": cnn, "network_forced": forced,
+                              "guess": diag,
+                              "speedup": zero["seconds"] / max(cnn["seconds"], 1e-9),
+                              "speedup_forced": zero["seconds"] / max(forced["seconds"], 1e-9)}
     peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"] \
         if (ROOT / "MEASURED_PEAKS.json").exists() else 1900.0
     line = {

@@ -576,19 +576,38 @@ def make_pairs(size: int, n: int, seed: int, rtol: float = 1e-6, batch: int = 64
     return PairSet(div, mask, inv, torch.cat(targets), torch.cat(rels), its)
 
 
+def network_guess(sim, net: UNet, mask: Optional[torch.Tensor]) -> torch.Tensor:
+    """The network's pressure prediction for the simulator's current system
+    (dense H x W float32, in the solver's pressure units)."""
+    H, W = sim.height, sim.width
+    pitch = sim.divergence.stride(0)
+    dfull = torch.zeros(1, H, pitch, dtype=torch.float32, device="cuda")
+    dfull[0, :, :W] = sim.divergence
+    m = None
+    if mask is not None:
+        m = torch.zeros(1, H, pitch, dtype=torch.uint8, device="cuda")
+        m[0, :, :W] = mask.view(H, -1)[:, :W]
+    inv = inv_scale_of(dfull[:, :, :W], m[:, :, :W] if m is not None else None)
+    p = net.forward(dfull, m, inv, H, W, pitch)
+    return (p[0] / inv[0]).contiguous()
+
+
 def warm_start_solve(sim, net: Optional[UNet], mask: Optional[torch.Tensor], rtol: float = 1e-4,
                      check: int = 100, max_sweeps: int = 200_000_000, fallback_sweeps: int = 10,
-                     time_limit_s: float = 120.0, regions: Optional[Regions] = None) -> dict:
+                     time_limit_s: float = 120.0, regions: Optional[Regions] = None,
+                     force: bool = False) -> dict:
     """Solve the pressure system of the simulator's last step to relative
     residual `rtol` with Jacobi sweeps, from zero (net None) or from the
     network's prediction.  Fallback rule: if the residual after
     `fallback_sweeps` sweeps from the prediction exceeds the residual after
-    as many sweeps from zero, restart from zero.  The residual is taken over
-    the fluid cells of `mask` (the obstacles the step used) with each
-    connected region's mean removed; obstacle cells, whose rows the sweep
-    updates but no fluid cell reads, are left out.  Labelling the regions
-    happens before the clock starts.  Returns sweeps, seconds, the residual
-    reached and whether the fallback fired."""
+    as many sweeps from zero, restart from zero; `force` skips the rule and
+    always sweeps from the prediction.  The residual is taken over the fluid
+    cells of `mask` (the obstacles the step used) with each connected
+    region's mean removed; obstacle cells, whose rows the sweep updates but
+    no fluid cell reads, are left out.  Labelling the regions happens before
+    the clock starts.  Returns sweeps, seconds, the residual reached, whether
+    the fallback fired and, with the rule, both arms' residuals after
+    `fallback_sweeps` sweeps."""
     import time
 
     from .. import _lib as L
@@ -615,17 +634,12 @@ def warm_start_solve(sim, net: Optional[UNet], mask: Optional[torch.Tensor], rto
         else:
             pv.copy_(p_dense)
 
-    if net is not None:
-        # pitched single-image copies, the layout the network input expects
-        dfull = torch.zeros(1, H, pitch, dtype=torch.float32, device="cuda")
-        dfull[0, :, :W] = sim.divergence
-        m = None
-        if mask is not None:
-            m = torch.zeros(1, H, pitch, dtype=torch.uint8, device="cuda")
-            m[0, :, :W] = mask.view(H, -1)[:, :W]
-        inv = inv_scale_of(dfull[:, :, :W], m[:, :, :W] if m is not None else None)
-        p = net.forward(dfull, m, inv, H, W, pitch)
-        guess = (p[0] / inv[0]).contiguous()
+    r_net = r_zero = None
+    if net is not None and force:
+        set_pressure(network_guess(sim, net, mask))
+        sweeps = 0
+    elif net is not None:
+        guess = network_guess(sim, net, mask)
         set_pressure(guess)
         sim.jacobi(fallback_sweeps)
         r_net = resid()
@@ -649,8 +663,65 @@ def warm_start_solve(sim, net: Optional[UNet], mask: Optional[torch.Tensor], rto
         sweeps += k
         res = resid()
     torch.cuda.synchronize()
-    return {"sweeps": sweeps, "seconds": time.perf_counter() - t0, "residual": res,
-            "fallback": used_fallback, "converged": res <= rtol}
+    out = {"sweeps": sweeps, "seconds": time.perf_counter() - t0, "residual": res,
+           "fallback": used_fallback, "converged": res <= rtol}
+    if r_net is not None:
+        out["residual_after_fallback_sweeps"] = {"network": r_net, "zero": r_zero}
+    return out
+
+
+def exact_pressure(sim, regions: Regions) -> torch.Tensor:
+    """FP64 conjugate-gradient solution of the simulator's current system to
+    relative residual 1e-8 (dense H x W float64, each fluid region's mean
+    removed, in the solver's pressure units)."""
+    H, W = sim.height, sim.width
+    P = _pitch(W)
+    div = torch.zeros(1, H, P, dtype=torch.float32, device="cuda")
+    div[0, :, :W] = sim.divergence
+    mask = torch.zeros(1, H, P, dtype=torch.uint8, device="cuda")
+    mask[0, :, :W] = (~regions.fluid).to(torch.uint8)
+    inv = inv_scale_of(div[:, :, :W], mask[:, :, :W])
+    p, _, _ = cg_solve(div, mask, inv, H, W, P, rtol=1e-8, max_iter=200000, regions=regions,
+                       as_double=True)
+    return p[0].double() / float(inv[0])
+
+
+def low_modes(e: torch.Tensor, kmax: int = 4) -> torch.Tensor:
+    """Coefficients of a field (H x W, zero on obstacles) on the domain's
+    slowest Neumann cosine modes cos(pi k (x + 1/2) / W) cos(pi l (y + 1/2) /
+    H), 0 <= k, l <= kmax, without the constant: the components that plain
+    Jacobi reduces slowest (their decay takes of the order of (W/pi)^2
+    sweeps)."""
+    H, W = e.shape
+    xs = (torch.arange(W, dtype=torch.float64, device=e.device) + 0.5) / W
+    ys = (torch.arange(H, dtype=torch.float64, device=e.device) + 0.5) / H
+    k = torch.arange(kmax + 1, dtype=torch.float64, device=e.device)
+    cx = torch.cos(math.pi * k[:, None] * xs[None, :])  # K x W
+    cy = torch.cos(math.pi * k[:, None] * ys[None, :])  # K x H
+    a = cy @ e.double() @ cx.T / (H * W)
+    a[0, 0] = 0.0
+    return a
+
+
+def guess_diagnostics(sim, net: UNet, mask: Optional[torch.Tensor], regions: Regions,
+                      exact: Optional[torch.Tensor] = None, kmax: int = 4) -> dict:
+    """How close the network's guess is to the exact solution, overall and on
+    the slowest modes, against the zero guess (whose error is the solution
+    itself): rel_error = ||P(g - x)|| / ||P(x)|| and low_mode_ratio =
+    ||low(P(g - x))|| / ||low(P(x))||, P removing each fluid region's mean
+    and zeroing obstacles.  A warm start cuts the sweeps to a residual target
+    only as far as it shrinks the low-mode error."""
+    H, W = sim.height, sim.width
+    if exact is None:
+        exact = exact_pressure(sim, regions)
+    g = network_guess(sim, net, mask).double()
+    ex = regions.project(exact.view(1, H, W))[0]
+    err = regions.project((g - exact).view(1, H, W))[0]
+    nx = float(ex.norm())
+    lx = float(low_modes(ex, kmax).norm())
+    return {"rel_error": float(err.norm()) / nx if nx > 0 else 0.0,
+            "low_mode_ratio": float(low_modes(err, kmax).norm()) / lx if lx > 0 else 0.0,
+            "kmax": kmax}
 
 
 def train(net: UNet, pairs: PairSet, steps: int, batch: int = 64, lr: float = 1e-3,
@@ -696,21 +767,14 @@ def project_divergence(sim, regions: Regions) -> float:
     return float(removed.abs().max()) / rms if rms > 0 else 0.0
 
 
-def fp32_floor(sim, regions: Regions) -> float:
+def fp32_floor(sim, regions: Regions, exact: Optional[torch.Tensor] = None) -> float:
     """Relative residual of the FP64 conjugate-gradient solution of the
     simulator's current system once rounded to FP32: the lowest residual a
     solver that stores the pressure in FP32 can reach.  Leaves the pressure
     field holding that rounded solution."""
-    H, W = sim.height, sim.width
-    P = _pitch(W)
-    div = torch.zeros(1, H, P, dtype=torch.float32, device="cuda")
-    div[0, :, :W] = sim.divergence
-    mask = torch.zeros(1, H, P, dtype=torch.uint8, device="cuda")
-    mask[0, :, :W] = (~regions.fluid).to(torch.uint8)
-    inv = inv_scale_of(div[:, :, :W], mask[:, :, :W])
-    p, _, _ = cg_solve(div, mask, inv, H, W, P, rtol=1e-8, max_iter=200000, regions=regions,
-                       as_double=True)
-    sim.pressure.copy_((p[0] / float(inv[0])).float())
+    if exact is None:
+        exact = exact_pressure(sim, regions)
+    sim.pressure.copy_(exact.float())
     labels, n = regions.image_labels(0)
     return sim.residual_regions(labels, n)
 

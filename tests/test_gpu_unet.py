@@ -372,7 +372,13 @@ def test_cg_targets_reach_tolerance(cuda, oracle):
 def test_training_reduces_loss_and_warm_start_gain(cuda, capsys):
     """Train on a small set of solver-generated pairs; the loss must drop, and
     on held-out steps the warm start (with its fallback rule) must never need
-    more sweeps than zero start; the measured gain is printed."""
+    more sweeps than zero start.  The test also records what the guess does:
+    sweeps with the guess forced (no fallback), both arms' residuals after
+    the 10 fallback sweeps (the rule must pick the lower) and the guess's
+    error on the slowest cosine modes relative to the zero guess's.  Those
+    modes set the sweep count, so a guess that leaves them (ratio >= 0.5)
+    cannot cut the sweeps (forced >= 0.9 x zero), and one that removes them
+    (ratio < 0.5) must show fewer sweeps than zero start."""
     import torch
 
     from natrix_gb300 import FluidSimulator
@@ -404,14 +410,26 @@ def test_training_reduces_loss_and_warm_start_gain(cuda, capsys):
         assert abs(float(b[sel].mean())) <= 1e-6 * float(b[sel].abs().max()) + 1e-12
     floor = ws.fp32_floor(sim, regions)
     assert floor < 1e-4, floor  # FP32 storage of the exact solution at 128x128
+    diag = ws.guess_diagnostics(sim, net, mask, regions)
     zero = ws.warm_start_solve(sim, None, mask, rtol=1e-3, check=50, time_limit_s=60,
                                regions=regions)
     warm = ws.warm_start_solve(sim, net, mask, rtol=1e-3, check=50, time_limit_s=60,
                                regions=regions)
+    forced = ws.warm_start_solve(sim, net, mask, rtol=1e-3, check=50, time_limit_s=60,
+                                 regions=regions, force=True)
+    r10 = warm["residual_after_fallback_sweeps"]
     with capsys.disabled():
         print(f"\nwarm start at {size}x{size}: zero {zero['sweeps']} sweeps, network "
-              f"{warm['sweeps']} sweeps (fallback {warm['fallback']}); loss {first:.4g} -> {last:.4g}")
-    assert zero["converged"] and warm["converged"]
+              f"{warm['sweeps']} sweeps (fallback {warm['fallback']}), forced guess "
+              f"{forced['sweeps']} sweeps; residual after 10 sweeps network {r10['network']:.3g} "
+              f"zero {r10['zero']:.3g}; guess error {diag['rel_error']:.3g}, low-mode error "
+              f"ratio {diag['low_mode_ratio']:.3g}; loss {first:.4g} -> {last:.4g}")
+    assert zero["converged"] and warm["converged"] and forced["converged"]
     # residuals are checked every 5% of the sweeps done, so counts agree to that
     assert warm["sweeps"] <= 1.06 * zero["sweeps"] + 10
+    assert warm["fallback"] == (r10["network"] > r10["zero"])
+    if diag["low_mode_ratio"] >= 0.5:
+        assert forced["sweeps"] >= 0.9 * zero["sweeps"], "a gain the slow modes do not explain"
+    else:
+        assert forced["sweeps"] < zero["sweeps"], "the slow modes shrank but the sweeps did not"
     sim.destroy()
