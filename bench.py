@@ -545,7 +545,7 @@ def other_configs(args) -> dict:
     b = batch_line(ns)
     out["batch_512"] = {k: b[k] for k in ("ms_per_step", "value", "unit",
                                           "hbm_roofline_model", "gpu_launches_per_step",
-                                          "persistent_launch")
+                                          "launch_per_phase")
                         if k in b}
     out["batch_512"]["workload"] = b["config"]["workload"]
     out["batch_512"]["steps"] = 20
@@ -643,8 +643,8 @@ def run_batch(args):
 
 def batch_line(args):
     """512 independent simulations (sides 64-512, 20/40/80 sweeps, 0-6 discs,
-    8 splats each per step): one graph-replayed launch per phase (the
-    default), the same step as one persistent launch, and looping the
+    8 splats each per step): one persistent launch per step (the default),
+    the same step as one graph-replayed launch per phase, and looping the
     single-grid simulator over the same simulations."""
     import torch
 
@@ -690,16 +690,16 @@ def batch_line(args):
         batch.sync()
         return e0.elapsed_time(e1) / args.steps, clocks.summary()
 
-    # the default (one graph-replayed launch per phase), then the same work
-    # as one persistent launch per step
-    batch.use_persistent(False)
+    # the default (one persistent launch per step), then the same work as
+    # one graph-replayed launch per phase
+    batch.use_persistent(True)
     tuning = batch.autotune()
     ms, clock_summary = timed(True)
     launches_total, per_step = batch.launches()
-    batch.use_persistent(True)
-    tuning_persistent = batch.autotune()
-    ms_persistent, _ = timed(False)
-    _, per_step_persistent = batch.launches()
+    batch.use_persistent(False)
+    tuning_phased = batch.autotune()
+    ms_phased, _ = timed(False)
+    _, per_step_phased = batch.launches()
     cells = float((sides.astype(np.float64) ** 2).sum())
     model_bytes = float(((sides.astype(np.float64) ** 2) * (92 + 13 * its)).sum())
     batch.destroy()
@@ -756,11 +756,10 @@ def batch_line(args):
                                "frac": model_bytes / (ms / 1e3) / 1e9 / peak, "peak_gbs": peak,
                                "peak_kind": peak_kind},
         "gpu_launches_per_step": per_step,
-        "persistent_launch": {"ms_per_step": ms_persistent,
-                              "value": cells / (ms_persistent / 1e3),
-                              "gpu_launches_per_step": per_step_persistent,
-                              "tuning": {str(c): list(v) for c, v in tuning_persistent.items()},
-                              "time_vs_per_phase": ms_persistent / ms},
+        "launch_per_phase": {"ms_per_step": ms_phased, "value": cells / (ms_phased / 1e3),
+                             "gpu_launches_per_step": per_step_phased,
+                             "tuning": {str(c): list(v) for c, v in tuning_phased.items()},
+                             "time_vs_persistent": ms_phased / ms},
         "looped_single_grid": None if loop_ms is None else {
             "ms_per_step": loop_ms, "value": cells / (loop_ms / 1e3),
             "speedup_of_batch": loop_ms / ms},

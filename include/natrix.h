@@ -223,10 +223,11 @@ int natrix_batch_set_tuning(natrix_batch* b, int32_t size_class, int32_t config,
                             int32_t sweeps_per_launch);
 /* Replay a captured CUDA graph per step (default 1) or launch directly (0). */
 int natrix_batch_set_graph(natrix_batch* b, int32_t enable);
-/* Step the whole batch in one persistent launch (1: resident CTAs claim the
- * step's work items in dependency order, each waiting for its simulation's
- * previous phase) or in one launch per phase (0, the default, faster on the
- * 512-simulation workload).  Both give the same values, bit for bit.  No
+/* Step the whole batch in one persistent launch (1, the default: resident
+ * CTAs claim the step's work items in dependency order, each waiting for its
+ * simulation's previous phase) or in one launch per phase (0).  Both give the
+ * same values, bit for bit.  The persistent step stages rows of at most 3008
+ * cells (wider simulations: NATRIX_ERANGE at the next step; use 0).  No
  * reference counterpart. */
 int natrix_batch_set_persistent(natrix_batch* b, int32_t enable);
 /* Queued per simulation for the next step (at most 256 ops and 256 shapes

@@ -42,7 +42,7 @@ class FluidBatch:
         self._handle = ctypes.c_void_p()
         call("natrix_batch_create", self.n, w, h, ctypes.byref(self._handle))
         self.tuning = {}
-        self.persistent = False
+        self.persistent = True
 
     @property
     def handle(self):
@@ -69,7 +69,7 @@ class FluidBatch:
         call("natrix_batch_set_graph", self.handle, 1 if enable else 0)
 
     def use_persistent(self, enable: bool):
-        """One persistent launch per step, or one launch per phase (default)."""
+        """One persistent launch per step (default), or one launch per phase."""
         call("natrix_batch_set_persistent", self.handle, 1 if enable else 0)
         self.persistent = bool(enable)
 
@@ -172,7 +172,7 @@ class FluidBatch:
         name = torch.cuda.get_device_name()
         hist = np.bincount([size_class(w, h) for w, h in zip(self.widths, self.heights)],
                            minlength=3)
-        mode = "persistent" if getattr(self, "persistent", False) else "per-phase"
+        mode = "persistent" if getattr(self, "persistent", True) else "per-phase"
         return (f"{name}|{mode}|classes={hist.tolist()}"
                 f"|cells={sum(w * h for w, h in zip(self.widths, self.heights))}")
 

@@ -264,224 +264,258 @@ __device__ __forceinline__ void step_tb_tile(const TileJob& job, unsigned char* 
     if (s_ok) tb_tile_body<C>(job, smem);
 }
 
-// Per-cell phases of the step kernel, K cells per thread: (x, y + 16 j),
-// j < K.  Every load of the K cells is issued before any of their
-// arithmetic (unconditional, in-bounds loads whose values the arithmetic may
-// not use), so each cell costs one round of L2 requests; the arithmetic is
-// the cell bodies' own helpers (cells.cuh), so the values are the same.
-// K = 1: with more cells in flight the kernel, capped at 128 registers by
-// the sweep tile, spills into the tile's sweep loop (measured: the sweep
-// items took twice as long).  Offsets are 32-bit: natrix_batch_create takes sides
-// of at most 32768 cells, so a simulation's offsets stay below 2^30.
-constexpr int kCellsPerThread = 1;
+// Per-cell phases of the step kernel (advection, divergence, gradient
+// subtraction, density advection) on a band of rows [a, b) of one
+// simulation.  Thread 0 brings the rows each phase reads into shared memory
+// with bulk asynchronous copies (one copy per field: a band of full pitched
+// rows is contiguous in global memory, and every field starts 256-byte
+// aligned with 128-byte rows), plus the halo rows the stencils and samplers
+// reach; the threads then compute from shared memory, one cell per thread
+// at a time.  A bilinear sample outside the staged rows (a backtrace longer
+// than the halo) reads global memory through L2.  The arithmetic is the cell
+// bodies' own helpers (cells.cuh), so the values are the same.  Offsets are
+// 32-bit: natrix_batch_create takes sides of at most 32768 cells, so a
+// simulation's offsets stay below 2^30.
+constexpr int kStageBytes = 192 * 1024;  // staging space of a band item
+constexpr int kAdvectHalo = 2;           // rows staged beyond a band for the samplers
 
-// Clamped neighbour offsets of cell (x, y) (common.sh:9-19).
-struct Nbr32 {
-    int c, l, r, b, t;
+// Rows of a staged band for a simulation of row pitch P: the largest
+// staging need per row is the gradient subtraction's 13 bytes per cell
+// (velocity, pressure, flags) plus the halo rows.
+// Widest row pitch whose band of one row and its halos fits the staging.
+constexpr int kMaxStagedPitch = kStageBytes / (13 * (1 + 2 * kAdvectHalo)) / 32 * 32;
+static_assert(kMaxStagedPitch >= 3008, "staging space for rows of 3008 cells");
+
+inline int staged_band_rows(int P) {
+    const int r = kStageBytes / (13 * P) - 2 * kAdvectHalo;
+    return r < 1 ? 1 : (r > 64 ? 64 : r);
+}
+
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes,
+                                          uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Thread 0 issues up to three row-range copies on the step barrier and
+// waits for them (bounded); every thread returns once they have landed.
+struct RowCopy {
+    unsigned char* dst;
+    const unsigned char* src;
+    uint32_t bytes;
 };
-__device__ __forceinline__ Nbr32 nbrs32(const Grid& g, int x, int y) {
-    Nbr32 n;
-    n.c = y * g.P + x;
-    n.l = x > 0 ? n.c - 1 : n.c;
-    n.r = x < g.W - 1 ? n.c + 1 : n.c;
-    n.b = y > 0 ? n.c - g.P : n.c;
-    n.t = y < g.H - 1 ? n.c + g.P : n.c;
-    return n;
+
+__device__ __forceinline__ void stage_rows(const RowCopy* c, int n, uint64_t* bar,
+                                           uint32_t* s_parity, int* status) {
+    if (threadIdx.x + 32 * threadIdx.y == 0) {
+        uint32_t total = 0;
+        for (int k = 0; k < n; ++k) total += c[k].bytes;
+        fence_before_tma();
+        mbar_expect_tx(bar, total);
+        for (int k = 0; k < n; ++k)
+            if (c[k].bytes) bulk_copy(c[k].dst, c[k].src, c[k].bytes, bar);
+        const uint32_t parity = *s_parity;
+        *s_parity ^= 1u;
+        if (!wait_phase(bar, parity)) {
+            atomicOr(status, 1);
+            wait_phase(bar, parity);
+        }
+    }
+    __syncthreads();
 }
 
-// vel_at with a 32-bit offset and an L2 load.
-__device__ __forceinline__ float2 vel_at32(const float2* v, const Grid& g, int x, int y,
-                                           bool zb) {
-    if (zb && (x == 0 || x == g.W - 1 || y == 0 || y == g.H - 1)) return make_float2(0.0f, 0.0f);
-    return __ldcg(v + y * g.P + x);
+// Rows [lo, hi) of a pitched field as a copy into shared memory at dst.
+template <class T>
+__device__ __forceinline__ RowCopy rows_of(unsigned char* dst, const T* field, const Grid& g,
+                                           int lo, int hi) {
+    return RowCopy{dst, reinterpret_cast<const unsigned char*>(field + (size_t)lo * g.P),
+                   (uint32_t)((hi - lo) * g.P * sizeof(T))};
 }
 
-__device__ __forceinline__ void band_advect(const BatchSimDesc* sd, float dt, int mask_zero, int a,
-                                         int b) {
-    const int tx = threadIdx.x, ty = threadIdx.y;
+__device__ __forceinline__ int align_up_256(int b) { return (b + 255) / 256 * 256; }
+
+// Obstacles and forcing of a band (rows [a, b), a multiple of 32 rows unless
+// it is the grid's last): the obstacle raster writes the mask; when the
+// band's velocity and density rows fit the staging space they are staged,
+// the queued ops applied in shared memory by the forcing body (through a
+// row-rebased pointer, so it indexes the staged rows with its grid
+// coordinates) and the rows written back; wider bands read and write the
+// fields in place (plain loads: forcing is a simulation's first phase in the
+// launch, so no other CTA has written these rows yet).
+constexpr int kForceRows = 2 * kStepThreadsY;  // rows per forcing block call
+
+__device__ __forceinline__ void band_force(const BatchSimDesc* sd, int a, int b,
+                                           const ShapeOp* shapes, int ns, const ForceOp* ops,
+                                           int no, int rc, unsigned char* smem, uint64_t* bar,
+                                           uint32_t* s_parity, int* status) {
     const Grid g = sd->g;
-    // the step scalars in registers (advect_corners reads dt and speed)
+    if (ns)
+        for (int by = a; by < b; by += kForceRows)
+            for (int bx = 0; bx < g.W; bx += BX)
+                block_obstacles<2, kStepThreadsY>(sd->mask, g, shapes, ns, 1, bx, by);
+    if (!no) return;
+    const int vbytes = align_up_256((b - a) * g.P * 8);
+    if (vbytes + (b - a) * g.P * 4 > kStageBytes) {
+        for (int by = a; by < b; by += kForceRows)
+            for (int bx = 0; bx < g.W; bx += BX)
+                block_forcing<2, kStepThreadsY, false>(sd->vel[0], g, sd->rho[rc], g, ops, no,
+                                                       bx, by);
+        return;
+    }
+    RowCopy c[2] = {rows_of(smem, sd->vel[0], g, a, b),
+                    rows_of(smem + vbytes, sd->rho[rc], g, a, b)};
+    stage_rows(c, 2, bar, s_parity, status);
+    float2* sv = reinterpret_cast<float2*>(smem) - (size_t)a * g.P;
+    float* sr = reinterpret_cast<float*>(smem + vbytes) - (size_t)a * g.P;
+    for (int by = a; by < b; by += kForceRows)
+        for (int bx = 0; bx < g.W; bx += BX)
+            block_forcing<2, kStepThreadsY, false>(sv, g, sr, g, ops, no, bx, by);
+    __syncthreads();
+    // the staged rows back to global memory, 16 bytes per thread and access
+    const int n4v = (b - a) * g.P / 2, n4r = (b - a) * g.P / 4;
+    const float4* s4 = reinterpret_cast<const float4*>(smem);
+    float4* v4 = reinterpret_cast<float4*>(sd->vel[0] + (size_t)a * g.P);
+    for (int i = threadIdx.x + 32 * threadIdx.y; i < n4v; i += 32 * kStepThreadsY) v4[i] = s4[i];
+    const float4* r4s = reinterpret_cast<const float4*>(smem + vbytes);
+    float4* r4 = reinterpret_cast<float4*>(sd->rho[rc] + (size_t)a * g.P);
+    for (int i = threadIdx.x + 32 * threadIdx.y; i < n4r; i += 32 * kStepThreadsY) r4[i] = r4s[i];
+}
+
+__device__ __forceinline__ void band_advect(const BatchSimDesc* sd, float dt, int mask_zero,
+                                            int a, int b, unsigned char* smem, uint64_t* bar,
+                                            uint32_t* s_parity, int* status) {
+    const Grid g = sd->g;
+    const int r0 = max(a - kAdvectHalo, 0), r1 = min(b + kAdvectHalo, g.H);
+    const float2* vin = sd->vel[0];
+    const float2* sv = reinterpret_cast<const float2*>(smem);
+    const uint8_t* sm = smem + align_up_256((r1 - r0) * g.P * 8);
+    RowCopy c[2] = {rows_of(smem, vin, g, r0, r1),
+                    rows_of(smem + align_up_256((r1 - r0) * g.P * 8), sd->mask, g, a, b)};
+    stage_rows(c, mask_zero ? 1 : 2, bar, s_parity, status);
     StepParams sp{};
     sp.dt = dt;
     sp.speed = sd->sp.speed;
-    sp.dissipation = sd->sp.dissipation;
-    sp.mask_zero = mask_zero;
+    const float diss = sd->sp.dissipation;
     const bool zb = sd->sp.has_borders != 0;
-    const float2* vin = sd->vel[0];
+    auto vel = [&](int x, int y) {
+        if (zb && (x == 0 || x == g.W - 1 || y == 0 || y == g.H - 1))
+            return make_float2(0.0f, 0.0f);
+        return (y >= r0 && y < r1) ? sv[(y - r0) * g.P + x] : __ldcg(vin + y * g.P + x);
+    };
     float2* vout = sd->vel[1];
-    const uint8_t* mask = sd->mask;
-#pragma unroll 1
-    for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
-#pragma unroll 1
-        for (int x = tx; x < g.W; x += BX) {
-            bool act[kCellsPerThread], obs[kCellsPerThread];
-            float2 vc[kCellsPerThread];
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; ++j) {
-                const int y = y0 + j * kStepThreadsY;
-                act[j] = y < b;
-                obs[j] = act[j] && !sp.mask_zero && __ldcg(mask + y * g.P + x);
-                vc[j] = act[j] ? vel_at32(vin, g, x, y, zb) : make_float2(0.0f, 0.0f);
+    for (int y = a + (int)threadIdx.y; y < b; y += kStepThreadsY)
+        for (int x = threadIdx.x; x < g.W; x += BX) {
+            if (!mask_zero && sm[(y - a) * g.P + x]) {
+                vout[y * g.P + x] = make_float2(0.0f, 0.0f);
+                continue;
             }
-            float2 q[kCellsPerThread][4];
-            Corners c[kCellsPerThread];
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; ++j) {
-                const int y = y0 + j * kStepThreadsY;
-                c[j] = advect_corners(vc[j], x, y, g, &sp);
-                if (act[j]) {
-                    q[j][0] = vel_at32(vin, g, c[j].lo_x, c[j].hi_y, zb);
-                    q[j][1] = vel_at32(vin, g, c[j].hi_x, c[j].hi_y, zb);
-                    q[j][2] = vel_at32(vin, g, c[j].lo_x, c[j].lo_y, zb);
-                    q[j][3] = vel_at32(vin, g, c[j].hi_x, c[j].lo_y, zb);
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; ++j) {
-                const int y = y0 + j * kStepThreadsY;
-                if (!act[j]) continue;
-                vout[y * g.P + x] =
-                    obs[j] ? make_float2(0.0f, 0.0f)
-                           : advect_mix(q[j][0], q[j][1], q[j][2], q[j][3], c[j], sp.dissipation);
-            }
+            const Corners q = advect_corners(vel(x, y), x, y, g, &sp);
+            vout[y * g.P + x] = advect_mix(vel(q.lo_x, q.hi_y), vel(q.hi_x, q.hi_y),
+                                           vel(q.lo_x, q.lo_y), vel(q.hi_x, q.lo_y), q, diss);
         }
 }
 
 __device__ __forceinline__ void band_divergence(const BatchSimDesc* sd, int mask_zero, int a,
-                                             int b) {
-    const int tx = threadIdx.x, ty = threadIdx.y;
+                                                int b, unsigned char* smem, uint64_t* bar,
+                                                uint32_t* s_parity, int* status) {
     const Grid g = sd->g;
-    const float2* v = sd->vel[sd->last];
-    const uint8_t* mask = sd->mask;
-    const bool mz = mask_zero != 0;
-#pragma unroll 1
-    for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
-#pragma unroll 1
-        for (int x = tx; x < g.W; x += BX) {
-            uint32_t m[kCellsPerThread];  // obstacle bits of l, r, b, t
-            float t[kCellsPerThread][4];
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; ++j) {
-                const int y = y0 + j * kStepThreadsY;
-                if (y >= b) continue;
-                const Nbr32 n = nbrs32(g, x, y);
-                m[j] = mz ? 0u
-                          : (__ldcg(mask + n.l) ? 1u : 0u) | (__ldcg(mask + n.r) ? 2u : 0u) |
-                                (__ldcg(mask + n.b) ? 4u : 0u) | (__ldcg(mask + n.t) ? 8u : 0u);
-                t[j][0] = __ldcg(v + n.l).x;
-                t[j][1] = __ldcg(v + n.r).x;
-                t[j][2] = __ldcg(v + n.b).y;
-                t[j][3] = __ldcg(v + n.t).y;
-            }
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; ++j) {
-                const int y = y0 + j * kStepThreadsY;
-                if (y >= b) continue;
-                const int c = y * g.P + x;
-                const bool ol = m[j] & 1u, orr = m[j] & 2u, ob = m[j] & 4u, ot = m[j] & 8u;
-                const float bv = divergence_of(ol ? 0.0f : t[j][0], orr ? 0.0f : t[j][1],
-                                               ob ? 0.0f : t[j][2], ot ? 0.0f : t[j][3]);
-                sd->div[c] = bv;
-                sd->flags[c] = nb_flags(x, y, g, ol, orr, ob, ot);
-                sd->p[0][c] = (0.0f - bv) * 0.25f;
-            }
+    const int r0 = max(a - 1, 0), r1 = min(b + 1, g.H);
+    const float2* sv = reinterpret_cast<const float2*>(smem);
+    const uint8_t* sm = smem + align_up_256((r1 - r0) * g.P * 8);
+    RowCopy c[2] = {rows_of(smem, sd->vel[sd->last], g, r0, r1),
+                    rows_of(smem + align_up_256((r1 - r0) * g.P * 8), sd->mask, g, r0, r1)};
+    stage_rows(c, mask_zero ? 1 : 2, bar, s_parity, status);
+    for (int y = a + (int)threadIdx.y; y < b; y += kStepThreadsY)
+        for (int x = threadIdx.x; x < g.W; x += BX) {
+            // clamped neighbours (common.sh:9-19) as staged offsets
+            const int xl = x > 0 ? x - 1 : x, xr = x < g.W - 1 ? x + 1 : x;
+            const int yb = y > 0 ? y - 1 : y, yt = y < g.H - 1 ? y + 1 : y;
+            const int rc = (y - r0) * g.P, rb = (yb - r0) * g.P, rt = (yt - r0) * g.P;
+            const bool ol = !mask_zero && sm[rc + xl], orr = !mask_zero && sm[rc + xr];
+            const bool ob = !mask_zero && sm[rb + x], ot = !mask_zero && sm[rt + x];
+            const float bv = divergence_of(ol ? 0.0f : sv[rc + xl].x, orr ? 0.0f : sv[rc + xr].x,
+                                           ob ? 0.0f : sv[rb + x].y, ot ? 0.0f : sv[rt + x].y);
+            const int o = y * g.P + x;
+            sd->div[o] = bv;
+            sd->flags[o] = nb_flags(x, y, g, ol, orr, ob, ot);
+            sd->p[0][o] = (0.0f - bv) * 0.25f;
         }
 }
 
-__device__ __forceinline__ void band_subgrad(const BatchSimDesc* sd, int a, int b) {
-    const int tx = threadIdx.x, ty = threadIdx.y;
+__device__ __forceinline__ void band_subgrad(const BatchSimDesc* sd, int a, int b,
+                                             unsigned char* smem, uint64_t* bar,
+                                             uint32_t* s_parity, int* status) {
     const Grid g = sd->g;
-    const float* p = sd->p[sd->p_final];
-    const float2* vin = sd->vel[sd->last];
-    const uint8_t* flags = sd->flags;
+    const int r0 = max(a - 1, 0), r1 = min(b + 1, g.H);
+    const int vbytes = align_up_256((b - a) * g.P * 8);
+    const int pbytes = align_up_256((r1 - r0) * g.P * 4);
+    const float2* sv = reinterpret_cast<const float2*>(smem);
+    const float* spp = reinterpret_cast<const float*>(smem + vbytes);
+    const uint8_t* sf = smem + vbytes + pbytes;
+    RowCopy c[3] = {rows_of(smem, sd->vel[sd->last], g, a, b),
+                    rows_of(smem + vbytes, sd->p[sd->p_final], g, r0, r1),
+                    rows_of(smem + vbytes + pbytes, sd->flags, g, a, b)};
+    stage_rows(c, 3, bar, s_parity, status);
     float2* vout = sd->vel[0];
-#pragma unroll 1
-    for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
-#pragma unroll 1
-        for (int x = tx; x < g.W; x += BX) {
-            uint8_t f[kCellsPerThread];
-            float pv[kCellsPerThread][5];
-            float2 vc[kCellsPerThread];
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; ++j) {
-                const int y = y0 + j * kStepThreadsY;
-                if (y >= b) continue;
-                const Nbr32 n = nbrs32(g, x, y);
-                f[j] = __ldcg(flags + n.c);
-                pv[j][0] = __ldcg(p + n.c);
-                pv[j][1] = __ldcg(p + n.l);
-                pv[j][2] = __ldcg(p + n.r);
-                pv[j][3] = __ldcg(p + n.b);
-                pv[j][4] = __ldcg(p + n.t);
-                vc[j] = __ldcg(vin + n.c);
-            }
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; ++j) {
-                const int y = y0 + j * kStepThreadsY;
-                if (y >= b) continue;
-                vout[y * g.P + x] = subtract_gradient_of(vc[j], f[j], pv[j][0], pv[j][1],
-                                                         pv[j][2], pv[j][3], pv[j][4]);
-            }
+    for (int y = a + (int)threadIdx.y; y < b; y += kStepThreadsY)
+        for (int x = threadIdx.x; x < g.W; x += BX) {
+            const int xl = x > 0 ? x - 1 : x, xr = x < g.W - 1 ? x + 1 : x;
+            const int yb = y > 0 ? y - 1 : y, yt = y < g.H - 1 ? y + 1 : y;
+            const int rc = (y - r0) * g.P;
+            const uint8_t f = sf[(y - a) * g.P + x];
+            vout[y * g.P + x] = subtract_gradient_of(
+                sv[(y - a) * g.P + x], f, spp[rc + x], spp[rc + xl], spp[rc + xr],
+                spp[(yb - r0) * g.P + x], spp[(yt - r0) * g.P + x]);
         }
 }
 
 // Density advection on a density grid of the velocity grid's size (the batch
 // keeps them equal); the obstacles are reset before it runs.
 __device__ __forceinline__ void band_density(const BatchSimDesc* sd, float dt, int rc, int a,
-                                          int b) {
-    const int tx = threadIdx.x, ty = threadIdx.y;
+                                             int b, unsigned char* smem, uint64_t* bar,
+                                             uint32_t* s_parity, int* status) {
     const Grid g = sd->g;
-    // the step scalars in registers (density_corners reads dt and the speed)
+    const int q0 = max(a - kAdvectHalo, 0), q1 = min(b + kAdvectHalo, g.H);  // density rows
+    const int v0 = max(a - 1, 0), v1 = min(b + 1, g.H);                     // velocity rows
+    const float* rin = sd->rho[rc];
+    const float2* v = sd->vel[0];
+    const int rbytes = align_up_256((q1 - q0) * g.P * 4);
+    const float* sr = reinterpret_cast<const float*>(smem);
+    const float2* sv = reinterpret_cast<const float2*>(smem + rbytes);
+    RowCopy c[2] = {rows_of(smem, rin, g, q0, q1), rows_of(smem + rbytes, v, g, v0, v1)};
+    stage_rows(c, 2, bar, s_parity, status);
     StepParams sp{};
     sp.dt = dt;
     sp.d_speed = sd->sp.d_speed;
-    sp.d_dissipation = sd->sp.d_dissipation;
-    const float* rin = sd->rho[rc];
+    const float diss = sd->sp.d_dissipation;
+    auto vel = [&](int x, int y) {
+        return (y >= v0 && y < v1) ? sv[(y - v0) * g.P + x] : __ldcg(v + y * g.P + x);
+    };
+    auto rho = [&](int x, int y) {
+        return (y >= q0 && y < q1) ? sr[(y - q0) * g.P + x] : __ldcg(rin + y * g.P + x);
+    };
     float* rout = sd->rho[1 - rc];
-    const float2* v = sd->vel[0];
-#pragma unroll 1
-    for (int y0 = a + ty; y0 < b; y0 += kCellsPerThread * kStepThreadsY)
-#pragma unroll 1
-        for (int x = tx; x < g.W; x += BX) {
-            float2 u[kCellsPerThread];
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; ++j) {
-                const int y = y0 + j * kStepThreadsY;
-                if (y >= b) continue;
-                const Corners cv = density_vel_corners(x, y, g, g);
-                const float2 q0 = __ldcg(v + cv.hi_y * g.P + cv.lo_x);
-                const float2 q1 = __ldcg(v + cv.hi_y * g.P + cv.hi_x);
-                const float2 q2 = __ldcg(v + cv.lo_y * g.P + cv.lo_x);
-                const float2 q3 = __ldcg(v + cv.lo_y * g.P + cv.hi_x);
-                if (on_centre(cv)) {
-                    u[j] = q2;
-                } else {  // sample_vel's arithmetic
-                    const float h1x = mixf(q0.x, q1.x, cv.dx), h1y = mixf(q0.y, q1.y, cv.dx);
-                    const float h2x = mixf(q2.x, q3.x, cv.dx), h2y = mixf(q2.y, q3.y, cv.dx);
-                    u[j] = make_float2(mixf(h2x, h1x, cv.dy), mixf(h2y, h1y, cv.dy));
-                }
+    for (int y = a + (int)threadIdx.y; y < b; y += kStepThreadsY)
+        for (int x = threadIdx.x; x < g.W; x += BX) {
+            const Corners cv = density_vel_corners(x, y, g, g);
+            float2 u;
+            if (on_centre(cv)) {
+                u = vel(cv.lo_x, cv.lo_y);
+            } else {  // sample_vel's arithmetic
+                const float2 lt = vel(cv.lo_x, cv.hi_y), rt = vel(cv.hi_x, cv.hi_y);
+                const float2 lb = vel(cv.lo_x, cv.lo_y), rb = vel(cv.hi_x, cv.lo_y);
+                const float h1x = mixf(lt.x, rt.x, cv.dx), h1y = mixf(lt.y, rt.y, cv.dx);
+                const float h2x = mixf(lb.x, rb.x, cv.dx), h2y = mixf(lb.y, rb.y, cv.dx);
+                u = make_float2(mixf(h2x, h1x, cv.dy), mixf(h2y, h1y, cv.dy));
             }
-            float r[kCellsPerThread][4];
-            Corners c[kCellsPerThread];
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; ++j) {
-                const int y = y0 + j * kStepThreadsY;
-                if (y >= b) continue;
-                c[j] = density_corners(u[j], x, y, g, g, &sp);
-                r[j][0] = __ldcg(rin + c[j].hi_y * g.P + c[j].lo_x);
-                r[j][1] = __ldcg(rin + c[j].hi_y * g.P + c[j].hi_x);
-                r[j][2] = __ldcg(rin + c[j].lo_y * g.P + c[j].lo_x);
-                r[j][3] = __ldcg(rin + c[j].lo_y * g.P + c[j].hi_x);
-            }
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; ++j) {
-                const int y = y0 + j * kStepThreadsY;
-                if (y >= b) continue;
-                // sample_scalar's arithmetic
-                const float h1 = mixf(r[j][0], r[j][1], c[j].dx);
-                const float h2 = mixf(r[j][2], r[j][3], c[j].dx);
-                rout[y * g.P + x] = mixf(h2, h1, c[j].dy) * sp.d_dissipation;
-            }
+            const Corners q = density_corners(u, x, y, g, g, &sp);
+            // sample_scalar's arithmetic
+            const float h1 = mixf(rho(q.lo_x, q.hi_y), rho(q.hi_x, q.hi_y), q.dx);
+            const float h2 = mixf(rho(q.lo_x, q.lo_y), rho(q.hi_x, q.lo_y), q.dx);
+            rout[y * g.P + x] = mixf(h2, h1, q.dy) * diss;
         }
 }
 
@@ -622,26 +656,14 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
         const int sim = a.items[k].sim;
         const BatchSimDesc* sd = a.desc + sim;
         switch (kind) {
-            case ITEM_FORCE: {
-                const int ra = a.items[k].a, rb = a.items[k].b;
-                const int ns = ss.sh_count[sim], no = ss.op_count[sim];
-                const Grid g = sd->g;
-                constexpr int kRows = 4 * kStepThreadsY;  // rows per block call
-                for (int by = ra; by < rb; by += kRows)
-                    for (int bx = 0; bx < g.W; bx += BX) {
-                        if (ns)
-                            block_obstacles<4, kStepThreadsY>(
-                                sd->mask, g, ss.shapes + ss.sh_begin[sim], ns, 1, bx, by);
-                        if (no)
-                            block_forcing<4, kStepThreadsY, true>(
-                                sd->vel[0], g, sd->rho[ss.rc], g, ss.ops + ss.op_begin[sim], no,
-                                bx, by);
-                    }
+            case ITEM_FORCE:
+                band_force(sd, a.items[k].a, a.items[k].b, ss.shapes + ss.sh_begin[sim],
+                           ss.sh_count[sim], ss.ops + ss.op_begin[sim], ss.op_count[sim], ss.rc,
+                           smem, &s_bar, &s_parity, a.status);
                 break;
-            }
             case ITEM_ADVECT:
                 band_advect(sd, ss.dt, ss.sh_count[sim] == 0 ? 1 : 0, a.items[k].a,
-                            a.items[k].b);
+                            a.items[k].b, smem, &s_bar, &s_parity, a.status);
                 break;
             case ITEM_CALC_VORT: {
                 const Grid g = sd->g;
@@ -669,7 +691,8 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
                 break;
             }
             case ITEM_DIV:
-                band_divergence(sd, ss.sh_count[sim] == 0 ? 1 : 0, a.items[k].a, a.items[k].b);
+                band_divergence(sd, ss.sh_count[sim] == 0 ? 1 : 0, a.items[k].a, a.items[k].b,
+                                smem, &s_bar, &s_parity, a.status);
                 break;
             case ITEM_JACOBI: {
                 const int config = a.items[k].config;
@@ -685,20 +708,24 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
                 break;
             }
             case ITEM_SUBGRAD:
-                band_subgrad(sd, a.items[k].a, a.items[k].b);
+                band_subgrad(sd, a.items[k].a, a.items[k].b, smem, &s_bar, &s_parity, a.status);
                 break;
             case ITEM_DENSITY:
                 // the fluid update resets the obstacles before the density
                 // update runs (natrix/core/fluid_simulator.py:267-280): no
                 // mask test
-                band_density(sd, ss.dt, ss.rc, a.items[k].a, a.items[k].b);
+                band_density(sd, ss.dt, ss.rc, a.items[k].a, a.items[k].b, smem, &s_bar,
+                             &s_parity, a.status);
                 break;
             default: break;
         }
         __syncthreads();  // the item's writes are done
         if (tid == 0) {
-            __threadfence();
-            atomicAdd(a.counters + a.items[k].done, 1ull);
+            // release pattern: every write of the item (ordered before this
+            // thread by the barrier), then the completion count
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+            asm volatile("red.relaxed.gpu.global.add.u64 [%0], 1;" ::"l"(a.counters + a.items[k].done)
+                         : "memory");
             s_item = (int)s_next;
         }
         __syncthreads();
@@ -773,9 +800,9 @@ struct natrix_batch {
     int* d_status = nullptr;
     int64_t launches = 0;
     int launches_per_step = 0;
-    // persistent step kernel (one launch per step) or one launch per phase
-    // (the default: faster on the 512-simulation workload)
-    bool persistent = false;
+    // persistent step kernel (one launch per step, the default) or one
+    // launch per phase
+    bool persistent = true;
     StepItem* d_items = nullptr;
     size_t items_cap = 0;
     int n_items = 0;
@@ -790,13 +817,18 @@ namespace {
 
 // The persistent kernel's work list: phases in order, within a phase the
 // simulations by decreasing sweep work (the longest dependency chains start
-// first), per simulation its bands of rows (per-cell phases: about 16k
-// cells, a multiple of 64 rows) or its sweep tiles.  Each item waits for all
+// first), per simulation its bands of rows (see band_rows) or its sweep
+// tiles.  Each item waits for all
 // items of its simulation's previous phase.
 int build_step_items(natrix_batch* b, const std::vector<int>& cfg_of,
                      const std::vector<int>& per_of, const std::vector<int>& launches_of,
                      int max_launches) {
     const int n = b->n;
+    for (int i = 0; i < n; ++i)
+        if (b->grids[i].P > kMaxStagedPitch)
+            return fail(NATRIX_ERANGE,
+                        "the persistent batch step stages rows of at most 3008 cells in shared "
+                        "memory; use the per-phase mode for wider simulations");
     const int kF = 0, kA = 1, kCV = 2, kAV = 3, kVS = 4, kD = 5, kJ = 6;
     const int kS = kJ + max_launches, kR = kS + 1, phases = kR + 1;
     std::vector<int> order(n);
@@ -806,12 +838,20 @@ int build_step_items(natrix_batch* b, const std::vector<int>& cfg_of,
         const double wy = (double)b->grids[y].W * b->grids[y].H * b->prm[y].iterations;
         return wx > wy;
     });
-    // bands of a multiple of 64 rows (the forcing item's block height)
-    auto band_rows = [](const Grid& g) {
-        const int r = (16384 / g.W) / 64 * 64;
-        return r < 64 ? 64 : r;
+    // forcing, vorticity and viscosity bands: a multiple of 32 rows (the
+    // forcing item's block height), about 16k cells and within the staging
+    // space where that allows; the staged phases' bands fit their rows (and
+    // halos) in the staging space
+    auto staged = [&](int ph) { return ph == kA || ph == kD || ph == kS || ph == kR; };
+    auto band_rows = [&](const Grid& g, int ph) {
+        if (staged(ph)) return staged_band_rows(g.P);
+        // forcing stages 12 B per cell (velocity, density) in 32-row blocks
+        const int r = std::min(16384 / g.W, kStageBytes / (12 * g.P)) / kForceRows * kForceRows;
+        return r < kForceRows ? kForceRows : r;
     };
-    auto bands = [&](const Grid& g) { return (g.H + band_rows(g) - 1) / band_rows(g); };
+    auto bands = [&](const Grid& g, int ph) {
+        return (g.H + band_rows(g, ph) - 1) / band_rows(g, ph);
+    };
     auto tiles = [&](int i) {
         int tx, ty;
         jacobi_tile(cfg_of[i], &tx, &ty);
@@ -834,8 +874,12 @@ int build_step_items(natrix_batch* b, const std::vector<int>& cfg_of,
         seq[i].push_back(kR);
     }
     auto count_of = [&](int i, int ph) {
-        return (ph >= kJ && ph < kS) ? tiles(i) : bands(b->grids[i]);
+        return (ph >= kJ && ph < kS) ? tiles(i) : bands(b->grids[i], ph);
     };
+    // Phase-major over all simulations: every phase offers many ready items.
+    // (Cutting the list into waves that fit in L2, all phases of a wave
+    // before the next, was measured: 5.2 ms per step instead of 2.8 on the
+    // 512-simulation workload, the CTAs idling on the chain inside a wave.)
     std::vector<StepItem> items;
     for (int ph = 0; ph < phases; ++ph) {
         for (int i : order) {
@@ -878,7 +922,7 @@ int build_step_items(natrix_batch* b, const std::vector<int>& cfg_of,
                         : ph == kD  ? ITEM_DIV
                         : ph == kS  ? ITEM_SUBGRAD
                                     : ITEM_DENSITY;
-            const int rows = band_rows(g);
+            const int rows = band_rows(g, ph);
             for (int y = 0; y < g.H; y += rows) {
                 StepItem t = base;
                 t.a = y;

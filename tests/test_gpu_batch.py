@@ -205,3 +205,22 @@ def test_batch_512_workload_equals_single_simulators(cuda):
     for s, d in singles:
         d.destroy()
         s.destroy()
+
+
+def test_persistent_step_refuses_rows_wider_than_its_staging(cuda):
+    """The persistent step stages rows of at most 3008 cells in shared
+    memory: a wider simulation gets NATRIX_ERANGE with a clear message (and
+    steps in the per-phase mode)."""
+    from natrix_gb300 import _lib
+    from natrix_gb300.core.batch import FluidBatch
+
+    batch = FluidBatch([3040, 64], [8, 64])
+    batch.set_params(-1, speed=5.0, iterations=3, dissipation=0.99, vorticity=0.0,
+                     viscosity=0.0)
+    with pytest.raises(_lib.NatrixError) as err:
+        batch.step(1 / 60)
+    assert err.value.code == _lib.NATRIX_ERANGE and "3008" in str(err.value)
+    batch.use_persistent(False)
+    batch.step(1 / 60)
+    batch.sync()
+    batch.destroy()
