@@ -310,10 +310,13 @@ def run_reference(args, spec):
 def measure_grid(spec: wl.Workload, steps: int, warmup: int, seed: int, barrier=None,
                  local: int = 0, sample_clocks: bool = True) -> dict:
     """One single-grid workload through the public API: `warmup` untimed
-    frames, `steps` frames between CUDA events on the launching stream (the
-    Jacobi phases bracketed by the library's own events), then `steps` more
-    frames end to end, each with its density frame read back into pinned
-    host memory.  Returns the times and the library's launch statistics."""
+    frames, `steps` frames between CUDA events on the launching stream, the
+    next `steps` frames again with the Jacobi phases also bracketed by the
+    library's own events (events between launches stop programmatic
+    dependent launch from overlapping them, so the step time is taken
+    without them), then `steps` more frames end to end, each with its
+    density frame read back into pinned host memory.  Returns the times and
+    the library's launch statistics of the second pass."""
     import torch
 
     from natrix_gb300 import FluidSimulator, SmoothParticlesArea, _lib
@@ -326,7 +329,7 @@ def measure_grid(spec: wl.Workload, steps: int, warmup: int, seed: int, barrier=
     sim.speed, sim.dissipation = spec.speed, spec.dissipation
     den.speed, den.dissipation = spec.speed, spec.dissipation
     obst = wl.workload_obstacles(seed, spec)
-    total = warmup + 2 * steps
+    total = warmup + 3 * steps
     forcing = [wl.step_forcing(seed, i, spec) for i in range(total)]
     stream = torch.cuda.current_stream()
 
@@ -344,8 +347,6 @@ def measure_grid(spec: wl.Workload, steps: int, warmup: int, seed: int, barrier=
 
     lib = _lib.load()
     stats = _lib.Stats()
-    lib.natrix_get_stats(sim.handle, stats, 1)
-    lib.natrix_set_timing(sim.handle, 1)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()
@@ -356,8 +357,23 @@ def measure_grid(spec: wl.Workload, steps: int, warmup: int, seed: int, barrier=
         ev1.record(stream)
         torch.cuda.synchronize()
     barrier()
-    lib.natrix_set_timing(sim.handle, 0)
     ms = ev0.elapsed_time(ev1)
+    sim.sync()
+
+    # the same number of frames with the Jacobi phases timed by the library
+    lib.natrix_get_stats(sim.handle, stats, 1)
+    lib.natrix_set_timing(sim.handle, 1)
+    ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    ev2.record(stream)
+    for i in range(warmup + steps, warmup + 2 * steps):
+        frame(i)
+    ev3.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    lib.natrix_set_timing(sim.handle, 0)
+    ms_phase_events = ev2.elapsed_time(ev3)
     _lib.check(lib.natrix_get_stats(sim.handle, stats, 1))
     sim.sync()
 
@@ -374,7 +390,7 @@ def measure_grid(spec: wl.Workload, steps: int, warmup: int, seed: int, barrier=
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
-    for k, i in enumerate(range(warmup + steps, total)):
+    for k, i in enumerate(range(warmup + 2 * steps, total)):
         if copied[k % 2] is not None:
             stream.wait_event(copied[k % 2])
         frame(i)
@@ -391,7 +407,8 @@ def measure_grid(spec: wl.Workload, steps: int, warmup: int, seed: int, barrier=
     sim.sync()
     den.destroy()
     sim.destroy()
-    return {"ms": ms, "ms_e2e": t_e2e * 1e3, "stats": stats, "clocks": clocks.summary()}
+    return {"ms": ms, "ms_phase_events": ms_phase_events, "ms_e2e": t_e2e * 1e3, "stats": stats,
+            "clocks": clocks.summary()}
 
 
 class _NoClocks:
@@ -427,7 +444,8 @@ def run_natrix(args, spec):
     ms, t_e2e, stats = m["ms"], m["ms_e2e"] / 1e3, m["stats"]
     launches = int(stats.kernel_launches)
 
-    ms, ms_e2e = replicas.max_over_ranks([ms, t_e2e * 1e3], device="cuda")
+    ms, ms_e2e, ms_ev = replicas.max_over_ranks([ms, t_e2e * 1e3, m["ms_phase_events"]],
+                                                device="cuda")
     value = replicas.whole_job_rate(cells * args.steps, world, ms / 1e3)
     e2e_value = replicas.whole_job_rate(cells * args.steps, world, ms_e2e / 1e3)
 
@@ -497,6 +515,12 @@ def run_natrix(args, spec):
                          if traffic else None,
                          "peak_kind": peak_kind,
                          "launch_ms": launch_ms, "sweeps_per_launch": sweeps_per_launch,
+                         # CUDA events around each step's Jacobi phase, in a
+                         # second timed pass of as many frames (the events
+                         # keep the phase's first and last launch from
+                         # overlapping their neighbours)
+                         "launch_ms_pass": {"steps": args.steps,
+                                            "ms_per_step": ms_ev / args.steps},
                          "bytes_per_launch": alg_bytes,
                          "bytes_model": ("13 B per cell per launch (pressure, divergence, "
                                          "flags read once; pressure written once), plus "

@@ -202,6 +202,11 @@ struct RtCfg {
 using RtA = RtCfg<8, 16, 8>;
 // 16 warps x 9 rows: 128x144 region, 112x128 output tile
 using RtB = RtCfg<9, 16, 8>;
+// 16 warps x 2 rows: 128x32 region, 112x16 output tile.  For grids with
+// fewer tall tiles than SMs: a sweep of a tile costs time in proportion to
+// the rows each warp holds, so more, shorter tiles finish a launch sooner
+// although each recomputes a larger share of halo cells.
+using RtC = RtCfg<2, 16, 8>;
 
 // The three copies of a tile on one mbarrier phase: the expected bytes are
 // registered first, so the phase cannot complete before the last copy lands

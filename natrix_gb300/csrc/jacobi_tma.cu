@@ -268,16 +268,17 @@ bool encode_2d(CUtensorMap* map, CUtensorMapDataType dt, int elem_bytes, void* b
     return true;
 }
 
-// NATRIX_JACOBI_VARIANT=0 forces the shared-memory kernel on every single
-// grid (for comparison runs); otherwise the tile shape is chosen by
-// jacobi_config.
-bool force_tb() {
-    static int v = -1;
-    if (v < 0) {
+// NATRIX_JACOBI_VARIANT forces one tile shape on every single grid (for
+// comparison runs): 0 the shared-memory kernel, 1 / 2 / 3 the register tiles
+// RtA / RtB / RtC (TB on grids at most 96 cells wide, which the register
+// tiles do not serve); otherwise the tile shape is chosen by jacobi_config.
+int forced_variant() {
+    static int v = -2;
+    if (v == -2) {
         const char* e = getenv("NATRIX_JACOBI_VARIANT");
-        v = (e && e[0] == '0') ? 1 : 0;
+        v = (e && e[0] >= '0' && e[0] <= '3' && e[1] == 0) ? e[0] - '0' : -1;
     }
-    return v == 1;
+    return v;
 }
 
 int num_sms() {
@@ -344,11 +345,28 @@ void box_of(int* bx, int* by, int* bfx) {
 
 int jacobi_max_sweeps_per_launch() { return Tb::HALO < RtA::HALO ? Tb::HALO : RtA::HALO; }
 
+// Time of one sweep launch in units of a row sweep on one SM: rounds of
+// tiles over the SMs times the region rows each tile sweeps.
+template <class C>
+long rt_latency(Grid g) {
+    const long tx = (g.W + C::TX - 1) / C::TX, ty = (g.H + C::TY - 1) / C::TY;
+    const long sms = num_sms();
+    return (tx * ty + sms - 1) / sms * C::RY;
+}
+
 int jacobi_config(Grid g) {
-    if (force_tb()) return JACOBI_TB;
+    const int forced = forced_variant();
+    if (forced == JACOBI_TB) return JACOBI_TB;
     // grids narrower than one register tile waste most of its 128 columns
     if (g.W <= 96) return JACOBI_TB;
-    return rt_cost<RtB>(g) < rt_cost<RtA>(g) ? JACOBI_RT_B : JACOBI_RT_A;
+    if (forced > 0) return forced;
+    const int tall = rt_cost<RtB>(g) < rt_cost<RtA>(g) ? JACOBI_RT_B : JACOBI_RT_A;
+    const long t_tall = tall == JACOBI_RT_B ? rt_latency<RtB>(g) : rt_latency<RtA>(g);
+    // short tiles where they shorten the launch (grids whose tall tiles
+    // leave most SMs idle).  Measured per step (eps 0.35, 12 discs; 256^2
+    // eps 0, no discs): 256^2 K40 68.0 -> 40.2 us, 512^2 K80 158.8 -> 113.5,
+    // 768^2 K80 171.4 -> 159.6; 1024^2 K40 113 with tall tiles, 138 short.
+    return rt_latency<RtC>(g) < t_tall ? JACOBI_RT_C : tall;
 }
 
 template <class C>
@@ -369,6 +387,8 @@ bool jacobi_tile_marks(int config, Grid g, TileMarks* out) {
         rt_marks<RtA>(g, &m);
     else if (config == JACOBI_RT_B)
         rt_marks<RtB>(g, &m);
+    else if (config == JACOBI_RT_C)
+        rt_marks<RtC>(g, &m);
     else
         return false;
     const long tiles = (long)m.tiles_x * m.tiles_y;
@@ -382,6 +402,7 @@ void jacobi_tile(int config, int* tx, int* ty) {
     switch (config) {
         case JACOBI_RT_A: *tx = RtA::TX; *ty = RtA::TY; break;
         case JACOBI_RT_B: *tx = RtB::TX; *ty = RtB::TY; break;
+        case JACOBI_RT_C: *tx = RtC::TX; *ty = RtC::TY; break;
         default: *tx = Tb::TX; *ty = Tb::TY; break;
     }
 }
@@ -393,6 +414,8 @@ bool jacobi_encode_maps_for(JacobiMaps* maps, int config, float* p0, float* p1, 
         box_of<RtA>(&bx, &by, &bfx);
     else if (config == JACOBI_RT_B)
         box_of<RtB>(&bx, &by, &bfx);
+    else if (config == JACOBI_RT_C)
+        box_of<RtC>(&bx, &by, &bfx);
     else
         box_of<Tb>(&bx, &by, &bfx);
     maps->config = config;
@@ -418,6 +441,7 @@ cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbu
     const bool pdl = pdl_enabled();
     if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st, pdl);
     if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st, pdl);
+    if (config == JACOBI_RT_C) return launch_rt_jobs<RtC>(jobs, status, st, pdl);
     return launch_tb_jobs<Tb>(jobs, status, st, pdl);
 }
 

@@ -261,70 +261,139 @@ __global__ void __launch_bounds__(BX* BY)
 }
 
 // Vorticity confinement in one pass: shader.CalcVorticity.comp then
-// shader.ApplyVorticity.comp on a 32 x 16 output tile.  The block stages the
-// velocity of the tile plus 2 cells (index-clamped, as GetNeighbours reads),
-// computes the curl of the tile plus 1 cell into shared memory (each at its
-// clamped grid position, so a clamped neighbour of an edge cell reads the edge
-// cell's own curl), then applies the confinement force.  Same expressions as
+// shader.ApplyVorticity.comp on a 64 x 32 output tile (each thread two
+// adjacent columns, four rows 8 apart).  The block stages the velocity of the
+// tile plus 2 cells (index-clamped, as GetNeighbours reads), computes the
+// curl of the tile plus 1 cell into shared memory (each at its clamped grid
+// position, so a clamped neighbour of an edge cell reads the edge cell's own
+// curl), then applies the confinement force.  Same expressions as
 // cell_calc_vorticity / cell_apply_vorticity, so the results are identical;
 // the curl of the tile is still written out (the vorticity field).
-constexpr int VT_W = BX, VT_H = BY * CPT;
+constexpr int VT_W = 2 * BX, VT_H = BY * CPT;
 constexpr int VV_W = VT_W + 4, VV_H = VT_H + 4;  // staged velocity
 constexpr int VW_W = VT_W + 2, VW_H = VT_H + 2;  // staged curl
+
+__device__ __forceinline__ float curl_at(const float2 (*sv)[VV_W], int cx, int cy) {
+    return 0.5f * ((sv[cy][cx + 1].y - sv[cy][cx - 1].y) - (sv[cy + 1][cx].x - sv[cy - 1][cx].x));
+}
+
+// shader.ApplyVorticity.comp:19-40 for one cell from its staged curls.
+__device__ __forceinline__ float2 confine(float wl, float wr, float wb, float wt, float wc,
+                                          float2 v, float vort, float dt) {
+    const float eps = 2.4414e-4f;
+    float fx = 0.5f * (fabsf(wt) - fabsf(wb));
+    float fy = 0.5f * (fabsf(wr) - fabsf(wl));
+    const float d = fx * fx + fy * fy;
+    const float m = eps > d ? eps : d;
+    // 1/sqrt(m) with both operations correctly rounded, as sqrtf and the IEEE
+    // division give (m >= eps is normal)
+    const float rs = __frcp_rn(__fsqrt_rn(m));
+    fx = fx * rs;
+    fy = fy * rs;
+    const float s = vort * wc;
+    fx = fx * (s * 1.0f);
+    fy = fy * (s * -1.0f);
+    return make_float2(v.x + fx * dt, v.y + fy * dt);
+}
+
+// Staging, curl and confinement of one tile.  INTERIOR: the tile plus its
+// 2-cell halo lies inside the grid, so no index is clamped, velocity rows are
+// staged as 16-byte pairs (x0 - 2 is even and rows are pitched to 32 cells)
+// and each thread's two cells are read and written as pairs; otherwise every
+// staged and sampled index is clamped to the grid as GetNeighbours clamps it.
+// Both paths evaluate the same expressions on the same values.
+template <bool INTERIOR>
+__device__ __forceinline__ void vorticity_tile(const float2* __restrict__ vin,
+                                               float2* __restrict__ vout, float* __restrict__ w,
+                                               const Grid& g, const StepParams* sp,
+                                               float2 (*sv)[VV_W], float (*sw)[VW_W], int x0,
+                                               int y0) {
+    const int lane = threadIdx.x, wy = threadIdx.y;
+    if (INTERIOR) {
+        const float4* src = reinterpret_cast<const float4*>(vin + (y0 - 2) * g.P + (x0 - 2));
+        const int qp = g.P / 2;
+        for (int ry = wy; ry < VV_H; ry += BY) {
+            *reinterpret_cast<float4*>(&sv[ry][2 * lane]) = __ldg(src + ry * qp + lane);
+            if (lane < VV_W / 2 - BX)
+                *reinterpret_cast<float4*>(&sv[ry][2 * BX + 2 * lane]) =
+                    __ldg(src + ry * qp + BX + lane);
+        }
+    } else {
+        for (int i = wy * BX + lane; i < VV_H * VV_W; i += BX * BY) {
+            const int ry = i / VV_W, rx = i % VV_W;
+            const int gx = min(max(x0 - 2 + rx, 0), g.W - 1), gy = min(max(y0 - 2 + ry, 0), g.H - 1);
+            sv[ry][rx] = __ldg(vin + gy * g.P + gx);
+        }
+    }
+    __syncthreads();
+    if (INTERIOR) {
+        for (int ry = wy; ry < VW_H; ry += BY) {
+            sw[ry][lane] = curl_at(sv, lane + 1, ry + 1);
+            sw[ry][lane + BX] = curl_at(sv, lane + BX + 1, ry + 1);
+        }
+        const int i = wy * BX + lane;  // the last two curl columns
+        if (i < 2 * VW_H) {
+            const int ry = i >> 1, rx = 2 * BX + (i & 1);
+            sw[ry][rx] = curl_at(sv, rx + 1, ry + 1);
+        }
+    } else {
+        for (int i = wy * BX + lane; i < VW_H * VW_W; i += BX * BY) {
+            const int ry = i / VW_W, rx = i % VW_W;
+            // curl at the clamped grid position, from its clamped neighbours,
+            // read at that position's staged velocity
+            const int gx = min(max(x0 - 1 + rx, 0), g.W - 1), gy = min(max(y0 - 1 + ry, 0), g.H - 1);
+            sw[ry][rx] = curl_at(sv, gx - x0 + 2, gy - y0 + 2);
+        }
+    }
+    __syncthreads();
+    const float vort = sp->vorticity, dt = sp->dt;
+    const int tx = 2 * lane;
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+        const int ty = wy + k * BY;
+        const int x = x0 + tx, y = y0 + ty;
+        if (INTERIOR) {
+            const float2 a = *reinterpret_cast<const float2*>(&sw[ty + 1][tx]);      // wl0, wc0
+            const float2 b = *reinterpret_cast<const float2*>(&sw[ty + 1][tx + 2]);  // wc1, wr1
+            const float4 v = *reinterpret_cast<const float4*>(&sv[ty + 2][tx + 2]);
+            const float2 o0 = confine(a.x, b.x, sw[ty][tx + 1], sw[ty + 2][tx + 1], a.y,
+                                      make_float2(v.x, v.y), vort, dt);
+            const float2 o1 = confine(a.y, b.y, sw[ty][tx + 2], sw[ty + 2][tx + 2], b.x,
+                                      make_float2(v.z, v.w), vort, dt);
+            const int c = y * g.P + x;
+            *reinterpret_cast<float4*>(vout + c) = make_float4(o0.x, o0.y, o1.x, o1.y);
+            *reinterpret_cast<float2*>(w + c) = make_float2(a.y, b.x);
+        } else {
+            if (y >= g.H) continue;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int xh = x + h, th = tx + h;
+                if (xh >= g.W) continue;
+                const int xl = max(xh - 1, 0) - x0 + 1, xr = min(xh + 1, g.W - 1) - x0 + 1;
+                const int yb = max(y - 1, 0) - y0 + 1, yt = min(y + 1, g.H - 1) - y0 + 1;
+                const float wc = sw[ty + 1][th + 1];
+                const int c = y * g.P + xh;
+                vout[c] = confine(sw[ty + 1][xl], sw[ty + 1][xr], sw[yb][th + 1], sw[yt][th + 1],
+                                  wc, sv[ty + 2][th + 2], vort, dt);
+                w[c] = wc;
+            }
+        }
+    }
+}
 
 __global__ void __launch_bounds__(BX* BY)
     k_vorticity(const float2* __restrict__ vin, float2* __restrict__ vout, float* __restrict__ w,
                 Grid g, const __grid_constant__ StepParams spv) {
     pdl_enter();
-    const StepParams* sp = &spv;
-    __shared__ float2 sv[VV_H][VV_W];
-    __shared__ float sw[VW_H][VW_W];
+    __shared__ __align__(16) float2 sv[VV_H][VV_W];
+    __shared__ __align__(16) float sw[VW_H][VW_W];
     const int x0 = blockIdx.x * VT_W, y0 = blockIdx.y * VT_H;
-    const int tid = threadIdx.y * BX + threadIdx.x;
-    for (int i = tid; i < VV_H * VV_W; i += BX * BY) {
-        const int ry = i / VV_W, rx = i % VV_W;
-        const int gx = min(max(x0 - 2 + rx, 0), g.W - 1), gy = min(max(y0 - 2 + ry, 0), g.H - 1);
-        sv[ry][rx] = __ldg(vin + gy * g.P + gx);
-    }
-    __syncthreads();
-    for (int i = tid; i < VW_H * VW_W; i += BX * BY) {
-        const int ry = i / VW_W, rx = i % VW_W;
-        // curl at the clamped grid position, from its clamped neighbours
-        const int gx = min(max(x0 - 1 + rx, 0), g.W - 1), gy = min(max(y0 - 1 + ry, 0), g.H - 1);
-        const int cx = gx - x0 + 2, cy = gy - y0 + 2;  // its staged velocity position
-        const float2 vl = sv[cy][cx - 1], vr = sv[cy][cx + 1], vb = sv[cy - 1][cx],
-                     vt = sv[cy + 1][cx];
-        sw[ry][rx] = 0.5f * ((vr.y - vl.y) - (vt.x - vb.x));
-    }
-    __syncthreads();
-    const float eps = 2.4414e-4f;
-    const float vort = sp->vorticity, dt = sp->dt;
-#pragma unroll
-    for (int k = 0; k < CPT; ++k) {
-        const int tx = threadIdx.x, ty = threadIdx.y + k * BY;
-        const int x = x0 + tx, y = y0 + ty;
-        if (x >= g.W || y >= g.H) continue;
-        const int xl = max(x - 1, 0) - x0 + 1, xr = min(x + 1, g.W - 1) - x0 + 1;
-        const int yb = max(y - 1, 0) - y0 + 1, yt = min(y + 1, g.H - 1) - y0 + 1;
-        const float wl = sw[ty + 1][xl], wr = sw[ty + 1][xr], wb = sw[yb][tx + 1],
-                    wt = sw[yt][tx + 1], wc = sw[ty + 1][tx + 1];
-        float fx = 0.5f * (fabsf(wt) - fabsf(wb));
-        float fy = 0.5f * (fabsf(wr) - fabsf(wl));
-        const float d = fx * fx + fy * fy;
-        const float m = eps > d ? eps : d;
-        // 1/sqrt(m) with both operations correctly rounded, as sqrtf and the
-        // IEEE division give (m >= eps is normal)
-        const float rs = __frcp_rn(__fsqrt_rn(m));
-        fx = fx * rs;
-        fy = fy * rs;
-        const float s = vort * wc;
-        fx = fx * (s * 1.0f);
-        fy = fy * (s * -1.0f);
-        const float2 v = sv[ty + 2][tx + 2];
-        const int c = y * g.P + x;
-        vout[c] = make_float2(v.x + fx * dt, v.y + fy * dt);
-        w[c] = wc;
-    }
+    const bool interior = x0 >= 2 && y0 >= 2 && x0 + VT_W + 2 <= g.W && y0 + VT_H + 2 <= g.H &&
+                          (g.P & 1) == 0;
+    if (interior)
+        vorticity_tile<true>(vin, vout, w, g, &spv, sv, sw, x0, y0);
+    else
+        vorticity_tile<false>(vin, vout, w, g, &spv, sv, sw, x0, y0);
 }
 
 // Row-streaming 5-point stencils (divergence, gradient subtraction).  A warp

@@ -3,7 +3,8 @@
 NATRIX_PDL=0 launches the step's kernels in plain stream order instead of
 with programmatic dependent launch; NATRIX_JACOBI_VARIANT=0 runs the sweeps
 with the shared-memory tile kernel on every grid (no register tiles, no tile
-deal, gradient subtraction in its own launch).  Each mode runs in a child
+deal, gradient subtraction in its own launch), 1 / 2 / 3 with one register
+tile shape (128x128, 128x144 or 128x32 regions) whatever the grid size.  Each mode runs in a child
 process on the same seeded workload and must reproduce the default run's
 velocity, pressure, divergence, vorticity and density bytes exactly."""
 from __future__ import annotations
@@ -63,8 +64,11 @@ def run_mode(env_extra):
     return json.loads(res.stdout.strip().splitlines()[-1])
 
 
-@pytest.mark.parametrize("env", [{"NATRIX_PDL": "0"}, {"NATRIX_JACOBI_VARIANT": "0"}],
-                         ids=["plain-stream-order", "shared-memory-sweeps"])
+@pytest.mark.parametrize("env", [{"NATRIX_PDL": "0"}, {"NATRIX_JACOBI_VARIANT": "0"},
+                                 {"NATRIX_JACOBI_VARIANT": "1"}, {"NATRIX_JACOBI_VARIANT": "2"},
+                                 {"NATRIX_JACOBI_VARIANT": "3"}],
+                         ids=["plain-stream-order", "shared-memory-sweeps", "register-tiles-a",
+                              "register-tiles-b", "register-tiles-c"])
 def test_launch_mode_bit_identical(cuda, env):
     base = run_mode({})
     alt = run_mode(env)
