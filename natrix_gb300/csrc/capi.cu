@@ -15,6 +15,7 @@
 //                has fewer sweeps than the tile halo, else its own launch)
 //   obstacle reset: recorded on the host, applied lazily (the next raster
 //                writes a fresh mask; until then kernels treat it as empty)
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -263,6 +264,39 @@ int flush_fluid(natrix_sim* s, cudaStream_t st, bool* border_zeroed = nullptr) {
     return flush_force_list(s, s->fq, s->vel[0], s->g, nullptr, Grid{}, st, border_zeroed);
 }
 
+// Sparse velocity forcing for a step (on unless NATRIX_SPARSE_FORCING=0).
+bool sparse_forcing_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("NATRIX_SPARSE_FORCING");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+// The start of a step: the queued obstacles, then the velocity ops over the
+// blocks they reach (launch_forcing_sparse) when that is possible, else over
+// the whole grid.  *clamp_deferred: the advection must clamp its reads;
+// *border_zeroed: the border holds zero.
+int flush_fluid_for_step(natrix_sim* s, cudaStream_t st, bool* border_zeroed,
+                         bool* clamp_deferred) {
+    *clamp_deferred = false;
+    int rc = flush_shapes(s, st);
+    if (rc) return rc;
+    if (sparse_forcing_enabled() && !s->fq.empty() && s->fq.size() <= (size_t)kMaxOpsPerLaunch) {
+        cudaError_t e = cudaSuccess;
+        if (launch_forcing_sparse(s->vel[0], s->g, s->fq.data(), (int)s->fq.size(),
+                                  s->prm.has_borders ? 1 : 0, st, &e)) {
+            NX_LAUNCH(s, e);
+            s->fq.clear();
+            *border_zeroed = s->prm.has_borders != 0;
+            *clamp_deferred = true;
+            return NATRIX_OK;
+        }
+    }
+    return flush_force_list(s, s->fq, s->vel[0], s->g, nullptr, Grid{}, st,
+                            s->prm.has_borders ? border_zeroed : nullptr);
+}
+
 int flush_density(natrix_density* d, cudaStream_t st) {
     return flush_force_list(d->fluid, d->fq, nullptr, Grid{}, d->rho[d->cur], d->g, st);
 }
@@ -509,14 +543,15 @@ int natrix_step(natrix_sim* s, float dt, void* stream) {
     if (!s->prm.simulate) return NATRIX_OK;
     DeviceGuard dg(s->device);
     cudaStream_t st = stream_of(s, stream);
-    bool border_zeroed = false;
-    int rc = flush_fluid(s, st, s->prm.has_borders ? &border_zeroed : nullptr);
+    bool border_zeroed = false, clamp_deferred = false;
+    int rc = flush_fluid_for_step(s, st, &border_zeroed, &clamp_deferred);
     if (rc) return rc;
     const bool mask_zero = s->mask_reset_pending;
     const StepParams sp = fluid_params(s, dt, mask_zero);
 
     const Grid g = s->g;
-    NX_LAUNCH(s, launch_advect(s->vel[0], s->vel[1], s->mask, g, sp, border_zeroed, st));
+    NX_LAUNCH(s, launch_advect(s->vel[0], s->vel[1], s->mask, g, sp, border_zeroed, st,
+                               clamp_deferred));
     int cur = 1;
     if (s->prm.vorticity > 0.0f) {
         NX_LAUNCH(s, launch_vorticity(s->vel[cur], s->vel[3 - cur], s->vort, g, sp, st));

@@ -125,9 +125,23 @@ cudaError_t launch_obstacles_blocks(uint8_t* mask, Grid g, const ShapeOp* ops, i
 // ops (takes effect when the list holds a velocity op).
 cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const ForceOp* ops,
                            int n, int zero_border, cudaStream_t st);
+// Velocity ops over the blocks their footprints reach plus (zero_border)
+// the blocks on the grid's edge, which get their border cells zeroed.  The
+// reference's first velocity op clamps every cell of the grid; outside the
+// listed blocks that clamp is left to the advection's reads (clamp_on_read),
+// which is exact because no op changes a cell there and clamping is
+// idempotent.  Returns false, launching nothing, when the list is unbounded
+// (too many blocks) or holds no velocity op; the caller then runs
+// launch_forcing.  Only for a step's own flush, whose next launch is the
+// advection: nothing else may read the velocity in between.
+bool launch_forcing_sparse(float2* vel, Grid gv, const ForceOp* ops, int n, int zero_border,
+                           cudaStream_t st, cudaError_t* err);
 // border_zeroed: vin's border cells already hold zero (no test on read).
+// clamp_on_read: clamp every velocity read to [-1, 1] (after
+// launch_forcing_sparse; needs border_zeroed or no borders).
 cudaError_t launch_advect(const float2* vin, float2* vout, const uint8_t* mask, Grid g,
-                          const StepParams& sp, bool border_zeroed, cudaStream_t st);
+                          const StepParams& sp, bool border_zeroed, cudaStream_t st,
+                          bool clamp_on_read = false);
 // calc + apply in one pass (same results); writes the curl to w
 cudaError_t launch_vorticity(const float2* vin, float2* vout, float* w, Grid g,
                              const StepParams& sp, cudaStream_t st);

@@ -89,6 +89,19 @@ __global__ void __launch_bounds__(BX* BY)
                               (t / tl.tiles_x) * BY * FORCE_ROWS);
 }
 
+// Velocity forcing over listed blocks (launch_forcing_sparse): the same
+// block body as k_forcing, so a listed block's cells come out identical.
+template <int CAP>
+__global__ void __launch_bounds__(BX* BY)
+    k_vforcing_tiles(float2* __restrict__ vel, Grid gv,
+                     const __grid_constant__ OpBlock<ForceOp, CAP> ob,
+                     const __grid_constant__ ForceTiles tl, int zero_border) {
+    pdl_enter();
+    const int t = tl.id[blockIdx.x];
+    block_forcing<FORCE_ROWS>(vel, gv, nullptr, Grid{}, ob.op, ob.n, (t % tl.tiles_x) * BX,
+                              (t / tl.tiles_x) * BY * FORCE_ROWS, zero_border != 0);
+}
+
 template <typename Op, int CAP>
 OpBlock<Op, CAP> op_block(const Op* ops, int n) {
     OpBlock<Op, CAP> ob;
@@ -102,7 +115,14 @@ OpBlock<Op, CAP> op_block(const Op* ops, int n) {
 // on read); false when has_borders is off or when this step's forcing launch
 // already wrote the zero border in place, as the reference's InitBoundaries
 // dispatch does before advecting.
-template <bool ZB>
+// CLAMP: the step's first velocity op clamped only the blocks it listed
+// (launch_forcing_sparse); every velocity read is clamped here instead, which
+// leaves the listed blocks' (already clamped) values unchanged.
+__device__ __forceinline__ float2 clamp_vel(float2 v) {
+    return make_float2(clampf(v.x, -1.0f, 1.0f), clampf(v.y, -1.0f, 1.0f));
+}
+
+template <bool ZB, bool CLAMP = false>
 __global__ void __launch_bounds__(BX* BY)
     k_advect(const float2* __restrict__ vin, float2* __restrict__ vout,
              const uint8_t* __restrict__ mask, Grid g, const __grid_constant__ StepParams sp) {
@@ -136,7 +156,7 @@ __global__ void __launch_bounds__(BX* BY)
             vout[i] = zero;
             continue;
         }
-        float2 vel = vc[k];
+        float2 vel = CLAMP ? clamp_vel(vc[k]) : vc[k];
         if (ZB && (xb || y == 0 || y == g.H - 1)) vel = zero;
         const float fx = (float)x - vel.x * dt * speed;
         const float fy = (float)y - vel.y * dt * speed;
@@ -144,6 +164,12 @@ __global__ void __launch_bounds__(BX* BY)
         const int rl = c.lo_y * g.P, rh = c.hi_y * g.P;
         float2 lt = __ldg(vin + rh + c.lo_x), rt = __ldg(vin + rh + c.hi_x);
         float2 lb = __ldg(vin + rl + c.lo_x), rb = __ldg(vin + rl + c.hi_x);
+        if (CLAMP) {
+            lt = clamp_vel(lt);
+            rt = clamp_vel(rt);
+            lb = clamp_vel(lb);
+            rb = clamp_vel(rb);
+        }
         if (ZB) {
             const bool bxl = c.lo_x == 0 || c.lo_x == g.W - 1;
             const bool bxh = c.hi_x == 0 || c.hi_x == g.W - 1;
@@ -859,6 +885,79 @@ cudaError_t launch_obstacles_blocks(uint8_t* mask, Grid g, const ShapeOp* ops, i
                          st, mask, g, op_block<ShapeOp, kMaxOpsPerLaunch>(ops, n), fresh, tl);
 }
 
+// Blocks holding a cell that a velocity op may change (its footprint box, two
+// cells wider than the in-kernel tests: the cone's radius, the Gaussian's 3r
+// cut), plus the edge blocks when the border is zeroed.  false when a list
+// holds no velocity op or more blocks than a launch can carry.
+bool velocity_force_tiles(const ForceOp* ops, int n, Grid gv, bool border, ForceTiles* tl) {
+    const int th = BY * FORCE_ROWS;
+    const int tx = (gv.W + BX - 1) / BX, ty = (gv.H + th - 1) / th;
+    if ((long)tx * ty > 65536) return false;
+    std::vector<uint8_t> hit((size_t)tx * ty, 0);
+    bool any_velocity = false;
+    for (int k = 0; k < n; ++k) {
+        const ForceOp& op = ops[k];
+        float reach;
+        if (op.kind == FORCE_GAUSS)
+            reach = 3.0f * op.r;
+        else if (op.kind == FORCE_CONE_VELOCITY)
+            reach = op.r;
+        else
+            return false;
+        any_velocity = true;
+        // a negative or NaN reach changes no cell (the kernel's tests fail)
+        if (!(reach >= 0.0f)) continue;
+        const double cx = (double)op.px * gv.W, cy = (double)op.py * gv.H, rr = (double)reach + 2.0;
+        const double fx0 = std::max(cx - rr, 0.0), fx1 = std::min(cx + rr, (double)(gv.W - 1));
+        const double fy0 = std::max(cy - rr, 0.0), fy1 = std::min(cy + rr, (double)(gv.H - 1));
+        if (!(fx0 <= fx1) || !(fy0 <= fy1)) continue;
+        for (int j = (int)fy0 / th; j <= (int)fy1 / th; ++j)
+            for (int i = (int)fx0 / BX; i <= (int)fx1 / BX; ++i) hit[(size_t)j * tx + i] = 1;
+    }
+    if (!any_velocity) return false;
+    if (border) {
+        for (int i = 0; i < tx; ++i) hit[i] = hit[(size_t)(ty - 1) * tx + i] = 1;
+        for (int j = 0; j < ty; ++j) hit[(size_t)j * tx] = hit[(size_t)j * tx + tx - 1] = 1;
+    }
+    tl->n = 0;
+    tl->tiles_x = tx;
+    for (size_t t = 0; t < hit.size(); ++t)
+        if (hit[t]) {
+            if (tl->n == kMaxRasterBlocks) return false;
+            tl->id[tl->n++] = (uint16_t)t;
+        }
+    return true;
+}
+
+template <int CAP>
+cudaError_t launch_velocity_tiles(float2* vel, Grid gv, const ForceOp* ops, int n,
+                                  const ForceTiles& tl, int zero_border, cudaStream_t st) {
+    if (tl.n == 0) return cudaSuccess;
+    return launch_kernel(pdl_enabled(), k_vforcing_tiles<CAP>, dim3(tl.n), dim3(BX, BY), 0, st,
+                         vel, gv, op_block<ForceOp, CAP>(ops, n), tl, zero_border);
+}
+
+bool launch_forcing_sparse(float2* vel, Grid gv, const ForceOp* ops, int n, int zero_border,
+                           cudaStream_t st, cudaError_t* err) {
+    *err = cudaSuccess;
+    if (n < 1 || n > kMaxOpsPerLaunch || !vel) return false;
+    // Below 1024 blocks the whole-grid launch is one or a few waves and the
+    // block list costs more host time than it saves (256x256, 8 splats:
+    // 40.0 us per step whole-grid, 42.6 us listed); above half the blocks
+    // the advection's clamps cost more than the blocks skipped.
+    const long blocks = (long)((gv.W + BX - 1) / BX) * ((gv.H + BY * FORCE_ROWS - 1) / (BY * FORCE_ROWS));
+    if (blocks < 1024) return false;
+    ForceTiles tl;
+    if (!velocity_force_tiles(ops, n, gv, zero_border != 0, &tl) || 2L * tl.n > blocks) return false;
+    if (n <= 16)
+        *err = launch_velocity_tiles<16>(vel, gv, ops, n, tl, zero_border, st);
+    else if (n <= 64)
+        *err = launch_velocity_tiles<64>(vel, gv, ops, n, tl, zero_border, st);
+    else
+        *err = launch_velocity_tiles<kMaxOpsPerLaunch>(vel, gv, ops, n, tl, zero_border, st);
+    return true;
+}
+
 cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const ForceOp* ops,
                            int n, int zero_border, cudaStream_t st) {
     if (n < 0 || n > kMaxOpsPerLaunch) return cudaErrorInvalidValue;
@@ -885,7 +984,13 @@ cudaError_t launch_forcing(float2* vel, Grid gv, float* rho, Grid gd, const Forc
 }
 
 cudaError_t launch_advect(const float2* vin, float2* vout, const uint8_t* mask, Grid g,
-                          const StepParams& sp, bool border_zeroed, cudaStream_t st) {
+                          const StepParams& sp, bool border_zeroed, cudaStream_t st,
+                          bool clamp_on_read) {
+    if (clamp_on_read) {
+        if (sp.has_borders && !border_zeroed) return cudaErrorInvalidValue;
+        return launch_kernel(pdl_enabled(), k_advect<false, true>, grid_cpt(g), dim3(BX, BY), 0,
+                             st, vin, vout, mask, g, sp);
+    }
     if (sp.has_borders && !border_zeroed)
         return launch_kernel(pdl_enabled(), k_advect<true>, grid_cpt(g), dim3(BX, BY), 0, st, vin,
                              vout, mask, g, sp);

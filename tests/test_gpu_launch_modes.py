@@ -4,7 +4,10 @@ NATRIX_PDL=0 launches the step's kernels in plain stream order instead of
 with programmatic dependent launch; NATRIX_JACOBI_VARIANT=0 runs the sweeps
 with the shared-memory tile kernel on every grid (no register tiles, no tile
 deal, gradient subtraction in its own launch), 1 / 2 / 3 with one register
-tile shape (128x128, 128x144 or 128x32 regions) whatever the grid size.  Each mode runs in a child
+tile shape (128x128, 128x144 or 128x32 regions) whatever the grid size;
+NATRIX_SPARSE_FORCING=0 applies a step's velocity ops over the whole grid
+instead of the blocks they reach (with the first op's clamp then done by the
+advection's reads).  Each mode runs in a child
 process on the same seeded workload and must reproduce the default run's
 velocity, pressure, divergence, vorticity and density bytes exactly."""
 from __future__ import annotations
@@ -29,7 +32,7 @@ sys.path.insert(0, sys.argv[1])
 from natrix_gb300 import FluidSimulator, SmoothParticlesArea, _lib
 from natrix_gb300 import workloads as wl
 
-W, H = 512, 384
+W, H = 1056, 1024  # over 1024 forcing blocks: the step lists the blocks its splats reach
 sim = FluidSimulator(W, H)
 den = SmoothParticlesArea(W, H, sim)
 sim.iterations, sim.vorticity, sim.viscosity = 40, 0.35, 0.0
@@ -57,6 +60,7 @@ def run_mode(env_extra):
     env = dict(os.environ)
     env.pop("NATRIX_PDL", None)
     env.pop("NATRIX_JACOBI_VARIANT", None)
+    env.pop("NATRIX_SPARSE_FORCING", None)
     env.update(env_extra)
     res = subprocess.run([sys.executable, "-c", SCRIPT, str(ROOT)], env=env,
                          capture_output=True, text=True, timeout=600)
@@ -66,9 +70,9 @@ def run_mode(env_extra):
 
 @pytest.mark.parametrize("env", [{"NATRIX_PDL": "0"}, {"NATRIX_JACOBI_VARIANT": "0"},
                                  {"NATRIX_JACOBI_VARIANT": "1"}, {"NATRIX_JACOBI_VARIANT": "2"},
-                                 {"NATRIX_JACOBI_VARIANT": "3"}],
+                                 {"NATRIX_JACOBI_VARIANT": "3"}, {"NATRIX_SPARSE_FORCING": "0"}],
                          ids=["plain-stream-order", "shared-memory-sweeps", "register-tiles-a",
-                              "register-tiles-b", "register-tiles-c"])
+                              "register-tiles-b", "register-tiles-c", "full-grid-forcing"])
 def test_launch_mode_bit_identical(cuda, env):
     base = run_mode({})
     alt = run_mode(env)
