@@ -162,6 +162,7 @@ enum StepItemKind : int {
     ITEM_DENSITY
 };
 
+// 48 bytes: three 16-byte cp.async copies move one into shared memory
 struct StepItem {
     int kind;
     int sim;
@@ -175,6 +176,7 @@ struct StepItem {
     int pad[2];
 };
 
+static_assert(sizeof(StepItem) % 16 == 0, "StepItem moves in 16-byte copies");
 constexpr int kStepThreadsY = 16;  // CTA of 32 x 16 threads (16 warps)
 using TbStep = TbCfg<64, 32, 8, kStepThreadsY>;  // Tb's tile on 512 threads
 static_assert(RtB::THREADS == 32 * kStepThreadsY && RtA::THREADS == 32 * kStepThreadsY,
@@ -610,6 +612,29 @@ __device__ __forceinline__ StepParams step_params(const BatchSimDesc* sd, const 
     return sp;
 }
 
+// Completion signals of finished items, held back so that one release fence
+// covers several (the fence waits for the CTA's stores to reach L2, about a
+// microsecond).  Owned by thread 0.  Flushed when kPending items are held,
+// before thread 0 waits on a counter that is not yet satisfied, and at the
+// end: a CTA never spins while it holds a signal, so holding them cannot
+// deadlock two CTAs that wait on each other's counters.
+constexpr int kPending = 4;
+
+struct PendingSignals {
+    int idx[kPending];
+    int n = 0;
+    __device__ __forceinline__ void flush(unsigned long long* counters) {
+        if (n == 0) return;
+        // release pattern: every write of the held items (ordered before this
+        // thread by the barrier that ended each of them), then the counts
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        for (int i = 0; i < n; ++i)
+            asm volatile("red.relaxed.gpu.global.add.u64 [%0], 1;" ::"l"(counters + idx[i])
+                         : "memory");
+        n = 0;
+    }
+};
+
 __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const StepArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t s_bar;
@@ -617,6 +642,9 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
     __shared__ long long s_next;
     __shared__ uint32_t s_parity;
     __shared__ StepShared ss;
+    // the current item's descriptor and the next one's, copied ahead by
+    // thread 0 (cp.async) while the current item runs
+    __shared__ __align__(16) StepItem s_w[2];
     const int tid = threadIdx.x + 32 * threadIdx.y;
     if (tid == 0) {
         const StepHeader* hdr = reinterpret_cast<const StepHeader*>(a.step);
@@ -635,39 +663,55 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
         mbar_init(&s_bar, 1);
         fence_barrier_init();
         s_item = (int)(atomicAdd(a.claim, 1ull) - ss.base);
+        if (s_item < a.n_items) s_w[0] = a.items[s_item];
         s_pref = 0;
         s_parity = 0;
     }
     __syncthreads();
-    for (;;) {
+    PendingSignals pend;  // thread 0's
+    for (int cur = 0;; cur ^= 1) {
         const int k = s_item;
         if (k >= a.n_items) break;
+        const StepItem& w = s_w[cur];
         unsigned long long next = 0;
         if (tid == 0) next = atomicAdd(a.claim, 1ull);  // in flight during the wait
         if (tid == 0) {
-            const StepItem w = a.items[k];
-            if (w.wait >= 0 &&
-                !wait_counter(a.counters + w.wait, (ss.epoch + 1) * (unsigned long long)w.need))
-                atomicOr(a.status, 2);
+            if (w.wait >= 0) {
+                const unsigned long long target = (ss.epoch + 1) * (unsigned long long)w.need;
+                if (ld_acquire_u64(a.counters + w.wait) < target) {
+                    pend.flush(a.counters);
+                    if (!wait_counter(a.counters + w.wait, target)) atomicOr(a.status, 2);
+                }
+            }
             s_next = (long long)(next - ss.base);
+            if (s_next < a.n_items) {
+                const char* src = reinterpret_cast<const char*>(a.items + s_next);
+                const unsigned dst = (unsigned)__cvta_generic_to_shared(&s_w[cur ^ 1]);
+#pragma unroll
+                for (int i = 0; i < (int)(sizeof(StepItem) / 16); ++i)
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst + 16 * i),
+                                 "l"(src + 16 * i)
+                                 : "memory");
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
         }
         __syncthreads();  // s_item read by all; dependency satisfied
-        const int kind = a.items[k].kind;
-        const int sim = a.items[k].sim;
+        const int kind = w.kind;
+        const int sim = w.sim;
         const BatchSimDesc* sd = a.desc + sim;
         switch (kind) {
             case ITEM_FORCE:
-                band_force(sd, a.items[k].a, a.items[k].b, ss.shapes + ss.sh_begin[sim],
+                band_force(sd, w.a, w.b, ss.shapes + ss.sh_begin[sim],
                            ss.sh_count[sim], ss.ops + ss.op_begin[sim], ss.op_count[sim], ss.rc,
                            smem, &s_bar, &s_parity, a.status);
                 break;
             case ITEM_ADVECT:
-                band_advect(sd, ss.dt, ss.sh_count[sim] == 0 ? 1 : 0, a.items[k].a,
-                            a.items[k].b, smem, &s_bar, &s_parity, a.status);
+                band_advect(sd, ss.dt, ss.sh_count[sim] == 0 ? 1 : 0, w.a,
+                            w.b, smem, &s_bar, &s_parity, a.status);
                 break;
             case ITEM_CALC_VORT: {
                 const Grid g = sd->g;
-                band_cells(a.items[k].a, a.items[k].b, g.W, [&](int x, int y) {
+                band_cells(w.a, w.b, g.W, [&](int x, int y) {
                     cell_calc_vorticity<true>(sd->vel[sd->vort_in], sd->vort, g, x, y);
                 });
                 break;
@@ -675,7 +719,7 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
             case ITEM_APPLY_VORT: {
                 const Grid g = sd->g;
                 const StepParams sp = step_params(sd, ss, sim);
-                band_cells(a.items[k].a, a.items[k].b, g.W, [&](int x, int y) {
+                band_cells(w.a, w.b, g.W, [&](int x, int y) {
                     cell_apply_vorticity<true>(sd->vel[sd->vort_in], sd->vel[sd->vort_out],
                                                sd->vort, g, &sp, x, y);
                 });
@@ -684,18 +728,18 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
             case ITEM_VISC: {
                 const Grid g = sd->g;
                 const StepParams sp = step_params(sd, ss, sim);
-                band_cells(a.items[k].a, a.items[k].b, g.W, [&](int x, int y) {
+                band_cells(w.a, w.b, g.W, [&](int x, int y) {
                     cell_viscosity<true>(sd->vel[sd->visc_in], sd->vel[sd->visc_out], g, &sp, x,
                                          y);
                 });
                 break;
             }
             case ITEM_DIV:
-                band_divergence(sd, ss.sh_count[sim] == 0 ? 1 : 0, a.items[k].a, a.items[k].b,
+                band_divergence(sd, ss.sh_count[sim] == 0 ? 1 : 0, w.a, w.b,
                                 smem, &s_bar, &s_parity, a.status);
                 break;
             case ITEM_JACOBI: {
-                const int config = a.items[k].config;
+                const int config = w.config;
                 const long long nk = s_next;
                 if (config == JACOBI_RT_B)
                     jacobi_item<RtB>(k, nk, a.items, a.n_items, a.jsims, a.counters,
@@ -708,28 +752,27 @@ __global__ void __launch_bounds__(32 * kStepThreadsY, 1) k_batch_step(const Step
                 break;
             }
             case ITEM_SUBGRAD:
-                band_subgrad(sd, a.items[k].a, a.items[k].b, smem, &s_bar, &s_parity, a.status);
+                band_subgrad(sd, w.a, w.b, smem, &s_bar, &s_parity, a.status);
                 break;
             case ITEM_DENSITY:
                 // the fluid update resets the obstacles before the density
                 // update runs (natrix/core/fluid_simulator.py:267-280): no
                 // mask test
-                band_density(sd, ss.dt, ss.rc, a.items[k].a, a.items[k].b, smem, &s_bar,
+                band_density(sd, ss.dt, ss.rc, w.a, w.b, smem, &s_bar,
                              &s_parity, a.status);
                 break;
             default: break;
         }
         __syncthreads();  // the item's writes are done
         if (tid == 0) {
-            // release pattern: every write of the item (ordered before this
-            // thread by the barrier), then the completion count
-            asm volatile("fence.acq_rel.gpu;" ::: "memory");
-            asm volatile("red.relaxed.gpu.global.add.u64 [%0], 1;" ::"l"(a.counters + a.items[k].done)
-                         : "memory");
+            pend.idx[pend.n++] = w.done;
+            if (pend.n == kPending) pend.flush(a.counters);
+            asm volatile("cp.async.wait_all;" ::: "memory");  // the next descriptor
             s_item = (int)s_next;
         }
         __syncthreads();
     }
+    if (tid == 0) pend.flush(a.counters);
 }
 
 constexpr int step_smem_bytes() {

@@ -399,6 +399,54 @@ def test_non_finite_inputs_match_oracle(cuda, oracle):
     sim.destroy()
 
 
+def test_sparse_forcing_defers_clamp_exactly(cuda, oracle):
+    """On a grid of 1024 forcing blocks a step's velocity ops run only over
+    the blocks they reach (plus the edge blocks) and the advection clamps its
+    reads instead of the first op's whole-grid clamp.  Velocities outside
+    [-1, 1], NaN and infinities far from every op (unlisted blocks), next to
+    the ops and on the border must come out as the oracle's whole-grid
+    forcing gives them: finite values bit for bit, NaNs in the same cells."""
+    from natrix_gb300 import _lib
+
+    W = H = 1024
+    sim, den, ref, rden = make_pair(oracle, W, H, iterations=6, vorticity=0.3, viscosity=0.0,
+                                    speed=5.0, dissipation=0.99)
+    rng = np.random.default_rng(23)
+    v = rng.uniform(-1.5, 1.5, (H, W, 2)).astype(np.float32)  # a third outside [-1, 1]
+    v[700, 100, 0] = np.nan          # far from the ops
+    v[900, 900, :] = np.inf
+    v[650, 300, 1] = -np.inf
+    v[205, 205, :] = np.nan          # inside the cone's footprint
+    v[0, 500, 0] = 7.0               # on the border (zeroed before the advection)
+    v[800, 0, 1] = np.nan
+    sim.upload(_lib.FIELD_VELOCITY, v)
+    ref.velocity[...] = v
+    splats = np.array([[0.2, 0.2, 6.0, 0.5, -0.3, 0.8],
+                       [0.75, 0.3, 9.0, -0.2, 0.4, 0.5]], np.float32)
+
+    def same(got, want, what):
+        got, want = np.asarray(got), np.asarray(want)
+        gn, wn = np.isnan(got), np.isnan(want)
+        assert np.array_equal(gn, wn), f"{what}: NaN cells differ ({gn.sum()} vs {wn.sum()})"
+        assert np.array_equal(got[~gn], want[~wn]), f"{what}: finite values differ"
+
+    for step in range(2):
+        for s in (sim, ref):
+            s.add_velocity((0.2, 0.2), (0.6, -0.4), 12.0)
+            s.add_circle_obstacle((0.55, 0.65), 20.0)
+        sim.add_splats(splats, den)
+        ref.add_splats(splats, rden)
+        sim.update(1 / 60)
+        den.update(1 / 60)
+        ref.update(1 / 60)
+        rden.update(1 / 60)
+        got, want = fields(sim, den), ref_fields(ref, rden)
+        for k, val in got.items():
+            same(val, want[k], f"{k} step {step}")
+    den.destroy()
+    sim.destroy()
+
+
 def test_float64_tolerance(cuda, oracle):
     """GPU float32 vs the float64 oracle after 1 and 10 steps, within the
     stated tolerance (tests/tolerances.py)."""
