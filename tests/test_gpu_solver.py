@@ -399,18 +399,21 @@ def test_non_finite_inputs_match_oracle(cuda, oracle):
     sim.destroy()
 
 
-def test_sparse_forcing_defers_clamp_exactly(cuda, oracle):
+@pytest.mark.parametrize("borders", [True, False])
+def test_sparse_forcing_defers_clamp_exactly(cuda, oracle, borders):
     """On a grid of 1024 forcing blocks a step's velocity ops run only over
-    the blocks they reach (plus the edge blocks) and the advection clamps its
-    reads instead of the first op's whole-grid clamp.  Velocities outside
-    [-1, 1], NaN and infinities far from every op (unlisted blocks), next to
-    the ops and on the border must come out as the oracle's whole-grid
-    forcing gives them: finite values bit for bit, NaNs in the same cells."""
+    the blocks they reach (plus the edge blocks when the border is zeroed)
+    and the advection clamps its reads instead of the first op's whole-grid
+    clamp.  Velocities outside [-1, 1], NaN and infinities far from every op
+    (unlisted blocks), next to the ops and on the border must come out as the
+    oracle's whole-grid forcing gives them: finite values bit for bit, NaNs
+    in the same cells."""
     from natrix_gb300 import _lib
 
     W = H = 1024
     sim, den, ref, rden = make_pair(oracle, W, H, iterations=6, vorticity=0.3, viscosity=0.0,
                                     speed=5.0, dissipation=0.99)
+    sim.has_borders = ref.has_borders = borders
     rng = np.random.default_rng(23)
     v = rng.uniform(-1.5, 1.5, (H, W, 2)).astype(np.float32)  # a third outside [-1, 1]
     v[700, 100, 0] = np.nan          # far from the ops
