@@ -80,7 +80,7 @@ class FluidBatch:
     def add_splats(self, sim, splats):
         arr = np.ascontiguousarray(splats, np.float32).reshape(-1, _lib.SPLAT_FLOATS)
         call("natrix_batch_add_splats", self.handle, int(sim),
-             arr.ctypes.data_as(ctypes.c_void_p), arr.shape[0])
+             arr.ctypes.data, arr.shape[0])
 
     def add_circle_obstacle(self, sim, position, radius, static=False):
         call("natrix_batch_add_circle_obstacle", self.handle, int(sim), position[0], position[1],
@@ -90,15 +90,13 @@ class FluidBatch:
         """All simulations' splats at once: counts[n], splats (sum(counts), 6)."""
         c = np.ascontiguousarray(counts, np.int32)
         arr = np.ascontiguousarray(splats, np.float32)
-        call("natrix_batch_add_splats_bulk", self.handle, c.ctypes.data_as(ctypes.c_void_p),
-             arr.ctypes.data_as(ctypes.c_void_p))
+        call("natrix_batch_add_splats_bulk", self.handle, c.ctypes.data, arr.ctypes.data)
 
     def add_circles_bulk(self, counts: np.ndarray, circles: np.ndarray):
         """All simulations' discs at once: counts[n], circles (sum(counts), 3)."""
         c = np.ascontiguousarray(counts, np.int32)
         arr = np.ascontiguousarray(circles, np.float32)
-        call("natrix_batch_add_circles_bulk", self.handle, c.ctypes.data_as(ctypes.c_void_p),
-             arr.ctypes.data_as(ctypes.c_void_p))
+        call("natrix_batch_add_circles_bulk", self.handle, c.ctypes.data, arr.ctypes.data)
 
     def step(self, dt: float):
         call("natrix_batch_step", self.handle, float(dt), _stream())

@@ -48,7 +48,14 @@ def _view(ptr: int, pitch: int, height: int, width: int, kind: str) -> torch.Ten
     return torch.as_tensor(arr, device="cuda")
 
 
+# The current stream's raw handle without building a torch.cuda.Stream object
+# (a step calls this every frame; torch keeps the accessor in its C module)
+_raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+
+
 def _stream() -> ctypes.c_void_p:
+    if _raw_stream is not None:
+        return ctypes.c_void_p(_raw_stream(torch.cuda.current_device()))
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
@@ -245,7 +252,7 @@ class FluidSimulator:
         arr = np.ascontiguousarray(splats, dtype=np.float32).reshape(-1, _lib.SPLAT_FLOATS)
         self._sync_params()
         dh = density.handle if density is not None else None
-        call("natrix_add_splats", self.handle, dh, arr.ctypes.data_as(ctypes.c_void_p),
+        call("natrix_add_splats", self.handle, dh, arr.ctypes.data,
              arr.shape[0])
 
     @property
