@@ -166,12 +166,13 @@ class FluidSimulator:
         return self._handle
 
     def _sync_params(self) -> None:
-        key = (float(self._speed), int(self._iterations), float(self._dissipation),
-               float(self._vorticity), float(self._viscosity), bool(self.has_borders),
-               bool(self.simulate), int(self.sweeps_per_launch))
+        # compared as given (the frame's common case is "unchanged"), converted
+        # only when pushed
+        key = (self._speed, self._iterations, self._dissipation, self._vorticity,
+               self._viscosity, self.has_borders, self.simulate, self.sweeps_per_launch)
         if key != self._pushed:
-            p = Params(key[0], key[1], key[2], key[3], key[4], int(key[5]), int(key[6]),
-                       key[7])
+            p = Params(float(key[0]), int(key[1]), float(key[2]), float(key[3]), float(key[4]),
+                       int(bool(key[5])), int(bool(key[6])), int(key[7]))
             call("natrix_set_params", self.handle, ctypes.byref(p))
             self._pushed = key
 

@@ -79,9 +79,10 @@ class SmoothParticlesArea:
         return self._handle
 
     def _sync_params(self) -> None:
-        key = (float(self._speed), float(self._dissipation), bool(self.simulate))
+        key = (self._speed, self._dissipation, self.simulate)
         if key != self._pushed:
-            call("natrix_density_set_params", self.handle, key[0], key[1], int(key[2]))
+            call("natrix_density_set_params", self.handle, float(key[0]), float(key[1]),
+                 int(bool(key[2])))
             self._pushed = key
 
     def add_particles(self, position: tuple, radius: float, strength: float):
