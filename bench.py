@@ -106,6 +106,23 @@ def step_floor_bytes_per_cell(spec: wl.Workload, sweep_launches: float, fused: f
     return b
 
 
+def issue_roof(instructions, launch_ms, clocks):
+    """Warp instructions issued per second by the sweep launch against the
+    SMs' issue limit (4 per SM per clock at the sampled SM clock)."""
+    import torch
+
+    if not instructions or not launch_ms:
+        return None
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    if not mhz:
+        return None
+    achieved = instructions / (launch_ms / 1e3)
+    peak = 4.0 * sms * mhz * 1e6
+    return {"warp_instructions_per_launch": instructions, "achieved_per_s": achieved,
+            "peak_per_s": peak, "frac": achieved / peak, "sm_mhz": mhz}
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -463,6 +480,7 @@ def run_natrix(args, spec):
                  LAUNCH_BYTES["fused_gradient"] * fused_per_launch) * cells
     achieved = alg_bytes / (launch_ms / 1e3) / 1e9
     traffic = load_traffic(spec)
+    instructions = load_instructions(spec)
     sweep_launches_per_step = jl / max(int(stats.timed_phases), 1)
     fused_per_step = int(stats.timed_fused) / max(int(stats.timed_phases), 1)
     floor_b = step_floor_bytes_per_cell(spec, sweep_launches_per_step, fused_per_step)
@@ -530,7 +548,11 @@ def run_natrix(args, spec):
                                          "flags read once; pressure written once), plus "
                                          "16 B per cell (velocity in and out) on the launch "
                                          "that also subtracts the gradient"),
-                         "traffic_source": "profiles/jacobi_rt_%dx%d.txt" % (W, H)},
+                         "traffic_source": "profiles/jacobi_rt_%dx%d.txt" % (W, H),
+                         # the issue roof the kernel is held under: warp
+                         # instructions per launch (same profile) over the
+                         # launch time, against 4 per SM and clock
+                         "issue": issue_roof(instructions, launch_ms, m["clocks"])},
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": cells * 4},
             "gpu_launches": launches,
@@ -591,6 +613,19 @@ def load_traffic(spec):
     vals = [float(line.split()[-1]) for line in p.read_text().splitlines()
             if "traffic (dram read + write) MB" in line]
     return sum(vals) / len(vals) * 1e6 if vals else None
+
+
+def load_instructions(spec):
+    """Warp instructions per Jacobi launch (smsp__inst_executed.sum) from the
+    same committed ncu summary, if any."""
+    p = ROOT / "profiles" / f"jacobi_rt_{spec.width}x{spec.height}.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        parts = line.split()
+        if parts[:1] == ["smsp__inst_executed.sum"] and len(parts) >= 3 and parts[2] == "M":
+            return float(parts[1]) * 1e6
+    return None
 
 
 def run_particles(args, spec):
