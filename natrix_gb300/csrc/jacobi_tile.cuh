@@ -387,8 +387,30 @@ __device__ __forceinline__ void rt_tile_body(const TileJob& job, unsigned char* 
         }
         const bool out_col = c0 >= C::HXP && c0 < C::HXP + C::TX;
         const int gx = job.tile_x + c0 - C::HXP;
+        auto in_tile = [&](int r) {
+            const int rr = r0 + r;
+            const int gy = job.tile_y + rr - C::HALO;
+            return out_col && rr >= C::HALO && rr < C::HALO + C::TY && gy < g.H && gx < g.W;
+        };
+        // the velocity of three rows in flight at once (vin is only read in
+        // this launch; the rows' stores would otherwise order each load after
+        // the previous row's stores)
+        constexpr int kRows = 3;
+        float4 va[kRows], vb[kRows];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
+            if (r % kRows == 0) {
+#pragma unroll
+                for (int i = 0; i < kRows; ++i) {
+                    va[i] = vb[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (r + i < R && in_tile(r + i)) {
+                        const size_t o =
+                            (size_t)(job.tile_y + r0 + r + i - C::HALO) * g.P + gx;
+                        va[i] = __ldg(reinterpret_cast<const float4*>(job.vin + o));
+                        vb[i] = __ldg(reinterpret_cast<const float4*>(job.vin + o + 2));
+                    }
+                }
+            }
             float cur[4], dn[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
@@ -399,14 +421,13 @@ __device__ __forceinline__ void rt_tile_body(const TileJob& job, unsigned char* 
             const float rgt = __shfl_down_sync(FULL, cur[0], 1);
             const int rr = r0 + r;
             const int gy = job.tile_y + rr - C::HALO;
-            if (out_col && rr >= C::HALO && rr < C::HALO + C::TY && gy < g.H && gx < g.W) {
+            if (in_tile(r)) {
                 const float L[4] = {lft, cur[0], cur[1], cur[2]};
                 const float Rn[4] = {cur[1], cur[2], cur[3], rgt};
                 const size_t o = (size_t)gy * g.P + gx;
-                const float4 va = *reinterpret_cast<const float4*>(job.vin + o);
-                const float4 vb = *reinterpret_cast<const float4*>(job.vin + o + 2);
-                float2 v[4] = {make_float2(va.x, va.y), make_float2(va.z, va.w),
-                               make_float2(vb.x, vb.y), make_float2(vb.z, vb.w)};
+                const float4 a4 = va[r % kRows], b4 = vb[r % kRows];
+                float2 v[4] = {make_float2(a4.x, a4.y), make_float2(a4.z, a4.w),
+                               make_float2(b4.x, b4.y), make_float2(b4.z, b4.w)};
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const uint32_t fb = f[r] >> (8 * j);
