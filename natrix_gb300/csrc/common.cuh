@@ -80,10 +80,12 @@ __device__ __forceinline__ T ldp(const T* p) {
 template <bool CG = false>
 __device__ __forceinline__ float2 sample_vel(const float2* __restrict__ v, int P,
                                              const Corners& c) {
-    const float2 lt = ldf<CG>(v + (size_t)c.hi_y * P + c.lo_x);
-    const float2 rt = ldf<CG>(v + (size_t)c.hi_y * P + c.hi_x);
-    const float2 lb = ldf<CG>(v + (size_t)c.lo_y * P + c.lo_x);
-    const float2 rb = ldf<CG>(v + (size_t)c.lo_y * P + c.hi_x);
+    // 32-bit cell offsets (grids stay below 2^31 cells)
+    const int rh = c.hi_y * P, rl = c.lo_y * P;
+    const float2 lt = ldf<CG>(v + (rh + c.lo_x));
+    const float2 rt = ldf<CG>(v + (rh + c.hi_x));
+    const float2 lb = ldf<CG>(v + (rl + c.lo_x));
+    const float2 rb = ldf<CG>(v + (rl + c.hi_x));
     const float h1x = mixf(lt.x, rt.x, c.dx), h1y = mixf(lt.y, rt.y, c.dx);
     const float h2x = mixf(lb.x, rb.x, c.dx), h2y = mixf(lb.y, rb.y, c.dx);
     return make_float2(mixf(h2x, h1x, c.dy), mixf(h2y, h1y, c.dy));
@@ -92,10 +94,12 @@ __device__ __forceinline__ float2 sample_vel(const float2* __restrict__ v, int P
 template <bool CG = false>
 __device__ __forceinline__ float sample_scalar(const float* __restrict__ s, int P,
                                                const Corners& c) {
-    const float lt = ldf<CG>(s + (size_t)c.hi_y * P + c.lo_x);
-    const float rt = ldf<CG>(s + (size_t)c.hi_y * P + c.hi_x);
-    const float lb = ldf<CG>(s + (size_t)c.lo_y * P + c.lo_x);
-    const float rb = ldf<CG>(s + (size_t)c.lo_y * P + c.hi_x);
+    // 32-bit cell offsets (grids stay below 2^31 cells)
+    const int rh = c.hi_y * P, rl = c.lo_y * P;
+    const float lt = ldf<CG>(s + (rh + c.lo_x));
+    const float rt = ldf<CG>(s + (rh + c.hi_x));
+    const float lb = ldf<CG>(s + (rl + c.lo_x));
+    const float rb = ldf<CG>(s + (rl + c.hi_x));
     const float h1 = mixf(lt, rt, c.dx);
     const float h2 = mixf(lb, rb, c.dx);
     return mixf(h2, h1, c.dy);
