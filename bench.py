@@ -37,6 +37,7 @@ import argparse
 import csv
 import ctypes
 import json
+import math
 import os
 import subprocess
 import sys
@@ -93,12 +94,13 @@ LAUNCH_BYTES = {
 }
 
 
-def step_floor_bytes_per_cell(spec: wl.Workload, sweep_launches: float, fused: float) -> float:
+def step_floor_bytes_per_cell(spec: wl.Workload, sweep_chunks: float, fused: float) -> float:
     """Attainable floor of one step with the launch structure run here:
-    sweep_launches sweep launches per step, `fused` of which (0 or 1) also
-    subtract the gradient."""
+    sweep_chunks chunks of up to 8 sweeps per step (each reads its inputs and
+    writes the pressure once), `fused` of which (0 or 1) also subtract the
+    gradient."""
     b = (LAUNCH_BYTES["forcing"] + LAUNCH_BYTES["advect"] + LAUNCH_BYTES["density_advect"]
-         + LAUNCH_BYTES["divergence"] + LAUNCH_BYTES["sweep_launch"] * sweep_launches
+         + LAUNCH_BYTES["divergence"] + LAUNCH_BYTES["sweep_launch"] * sweep_chunks
          + LAUNCH_BYTES["fused_gradient"] * fused
          + LAUNCH_BYTES["subtract_gradient"] * (1.0 - fused))
     if spec.vorticity > 0:
@@ -476,14 +478,31 @@ def run_natrix(args, spec):
     # fuses; a launch that also subtracts the pressure gradient (the last of
     # a step when fused) reads and writes the velocity as well.
     fused_per_launch = int(stats.timed_fused) / jl
-    alg_bytes = (LAUNCH_BYTES["sweep_launch"] +
+    # a chunk is the up to 8 sweeps a tile keeps on chip; on grids with a
+    # tile for every SM one persistent launch runs all chunks of a step
+    chunks_per_launch = max(1, math.ceil(sweeps_per_launch / 8 - 1e-9))
+    chain = chunks_per_launch > 1
+    alg_bytes = (LAUNCH_BYTES["sweep_launch"] * chunks_per_launch +
                  LAUNCH_BYTES["fused_gradient"] * fused_per_launch) * cells
     achieved = alg_bytes / (launch_ms / 1e3) / 1e9
-    traffic = load_traffic(spec)
-    instructions = load_instructions(spec)
+    profile = ("jacobi_chain_%dx%d.txt" if chain else "jacobi_rt_%dx%d.txt") % (W, H)
+    traffic = load_traffic(profile)
+    instructions = load_instructions(profile)
     sweep_launches_per_step = jl / max(int(stats.timed_phases), 1)
+    chunks_per_step = sweep_launches_per_step * chunks_per_launch
     fused_per_step = int(stats.timed_fused) / max(int(stats.timed_phases), 1)
-    floor_b = step_floor_bytes_per_cell(spec, sweep_launches_per_step, fused_per_step)
+    floor_b = step_floor_bytes_per_cell(spec, chunks_per_step, fused_per_step)
+    if chain:
+        kernel_desc = ("jacobi sweep chain: every 8-sweep chunk of the step in one persistent "
+                       "launch (TMA tiles; a tile waits for its 3x3 neighbours' previous chunk)")
+        bytes_model = ("13 B per cell per chunk (pressure, divergence, flags read once; "
+                       "pressure written once), plus 16 B per cell (velocity in and out) on "
+                       "the last chunk, which also subtracts the gradient")
+    else:
+        kernel_desc = "jacobi sweep launch (temporally blocked, TMA tiles)"
+        bytes_model = ("13 B per cell per launch (pressure, divergence, flags read once; "
+                       "pressure written once), plus 16 B per cell (velocity in and out) on "
+                       "the launch that also subtracts the gradient")
 
     if rank == 0:
         # per-frame host->device bytes (carried in the launches' parameter
@@ -509,6 +528,7 @@ def run_natrix(args, spec):
             "hbm_roofline_step": {
                 "bytes_per_cell_step": floor_b,
                 "sweep_launches_per_step": sweep_launches_per_step,
+                "sweep_chunks_per_step": chunks_per_step,
                 "achieved_gbs": value * floor_b / 1e9,
                 "frac": value * floor_b / 1e9 / peak,
                 "peak_gbs": peak, "peak_kind": peak_kind,
@@ -524,12 +544,12 @@ def run_natrix(args, spec):
             "jacobi_cell_sweeps_per_s": {
                 "per_step_time": value * spec.iterations,
                 "per_jacobi_time": cells * sweeps_per_launch / (launch_ms / 1e3) * world},
-            "roofline": {"kernel": "jacobi sweep launch (temporally blocked, TMA tiles)",
+            "roofline": {"kernel": kernel_desc,
                          "bound": "hbm",
                          # what the kernel's time is spent on (its profile):
                          # the HBM fraction below is of its algorithmic bytes
                          "limiter": "FP32 issue and the per-sweep CTA barrier (8 sweeps "
-                                    "on chip per launch), not DRAM",
+                                    "on chip per chunk), not DRAM",
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "dram_gbs": (traffic / (launch_ms / 1e3) / 1e9) if traffic else None,
@@ -537,6 +557,7 @@ def run_natrix(args, spec):
                          if traffic else None,
                          "peak_kind": peak_kind,
                          "launch_ms": launch_ms, "sweeps_per_launch": sweeps_per_launch,
+                         "chunks_per_launch": chunks_per_launch,
                          # CUDA events around each step's Jacobi phase, in a
                          # second timed pass of as many frames (the events
                          # keep the phase's first and last launch from
@@ -544,11 +565,8 @@ def run_natrix(args, spec):
                          "launch_ms_pass": {"steps": args.steps,
                                             "ms_per_step": ms_ev / args.steps},
                          "bytes_per_launch": alg_bytes,
-                         "bytes_model": ("13 B per cell per launch (pressure, divergence, "
-                                         "flags read once; pressure written once), plus "
-                                         "16 B per cell (velocity in and out) on the launch "
-                                         "that also subtracts the gradient"),
-                         "traffic_source": "profiles/jacobi_rt_%dx%d.txt" % (W, H),
+                         "bytes_model": bytes_model,
+                         "traffic_source": "profiles/" + profile,
                          # the issue roof the kernel is held under: warp
                          # instructions per launch (same profile) over the
                          # launch time, against 4 per SM and clock
@@ -604,10 +622,11 @@ def other_configs(args) -> dict:
     return out
 
 
-def load_traffic(spec):
+def load_traffic(profile):
     """DRAM bytes (read + write) per Jacobi launch from the committed ncu
-    summary of this grid size (profiles/jacobi_rt_<W>x<H>.txt), if any."""
-    p = ROOT / "profiles" / f"jacobi_rt_{spec.width}x{spec.height}.txt"
+    summary `profiles/<profile>` (jacobi_rt_<W>x<H>.txt for the launch per
+    chunk, jacobi_chain_<W>x<H>.txt for the one-launch chain), if any."""
+    p = ROOT / "profiles" / profile
     if not p.exists():
         return None
     vals = [float(line.split()[-1]) for line in p.read_text().splitlines()
@@ -615,10 +634,10 @@ def load_traffic(spec):
     return sum(vals) / len(vals) * 1e6 if vals else None
 
 
-def load_instructions(spec):
+def load_instructions(profile):
     """Warp instructions per Jacobi launch (smsp__inst_executed.sum) from the
     same committed ncu summary, if any."""
-    p = ROOT / "profiles" / f"jacobi_rt_{spec.width}x{spec.height}.txt"
+    p = ROOT / "profiles" / profile
     if not p.exists():
         return None
     for line in p.read_text().splitlines():

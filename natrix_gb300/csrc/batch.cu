@@ -195,30 +195,6 @@ struct StepArgs {
     int* status;
 };
 
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Bounded wait (about 2^24 polls with back-off) for *c >= target.
-__device__ __forceinline__ bool wait_counter(const unsigned long long* c,
-                                             unsigned long long target) {
-    for (int it = 0; it < (1 << 24); ++it) {
-        if (ld_acquire_u64(c) >= target) return true;
-        __nanosleep(64);
-    }
-    return false;
-}
-
-// Order generic-proxy writes (other CTAs' stores released through a
-// completion counter; this CTA's use of the staging memory) before the
-// async-proxy copies the calling thread issues next.
-__device__ __forceinline__ void fence_before_tma() {
-    asm volatile("fence.proxy.async.global;" ::: "memory");
-    fence_proxy_async();
-}
-
 // A register tile of the step kernel.  `issued`: its copies were already
 // issued (prefetched during the previous item).  Once the tile sits in
 // registers, `prefetch()` may issue the next item's copies into the freed

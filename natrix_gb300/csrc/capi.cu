@@ -104,6 +104,11 @@ struct natrix_sim {
     TileMarks marks{};             // sweep tiles next to obstacles (geometry; words = 0: off)
     uint32_t* d_marks[2] = {};     // this step's marks / the previous step's
     int marks_cur = 0;
+    // counters of the one-launch sweep phase (launch_jacobi_chain) and their
+    // values after the last such launch
+    unsigned* d_chain = nullptr;
+    int chain_words = 0;
+    unsigned chain_claims = 0, chain_done = 0;
     std::vector<ForceOp> fq;
     std::vector<ShapeOp> sq;
     bool mask_reset_pending = true;  // the mask memory does not hold the current obstacles
@@ -159,6 +164,7 @@ void free_sim(natrix_sim* s) {
     cudaFree(s->d_maps);
     cudaFree(s->d_marks[0]);
     cudaFree(s->d_marks[1]);
+    cudaFree(s->d_chain);
     if (s->h_res) cudaFreeHost(s->h_res);
     delete s;
 }
@@ -301,6 +307,16 @@ int flush_density(natrix_density* d, cudaStream_t st) {
     return flush_force_list(d->fluid, d->fq, nullptr, Grid{}, d->rho[d->cur], d->g, st);
 }
 
+// NATRIX_JACOBI_CHAIN=0 runs a step's sweeps as one launch per chunk of the
+// tile halo instead of one persistent launch.
+bool jacobi_chain_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("NATRIX_JACOBI_CHAIN");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 // `sweeps` Jacobi sweeps in launches of sweeps_per_launch.  With vin / vout
 // the gradient subtraction rides on the last launch when that launch can
 // take it (register-tiled tiles, fewer sweeps than the halo); *fused says
@@ -318,6 +334,17 @@ int run_jacobi(natrix_sim* s, int sweeps, cudaStream_t st, const float2* vin = n
     }
     int launches = 0, total = sweeps;
     bool fuse_last = false;
+    if (vin && s->prm.sweeps_per_launch == 0 && s->d_chain && jacobi_chain_enabled()) {
+        // a step's sweeps: one persistent launch for every chunk
+        const int chunks = (sweeps + default_sweeps() - 1) / default_sweeps();
+        NX_LAUNCH(s, launch_jacobi_chain(s->d_maps, s->maps.config, s->p, s->p_cur, s->g, sweeps,
+                                         s->d_marks[s->marks_cur], vin, vout, s->d_chain,
+                                         &s->chain_claims, &s->chain_done, &fuse_last,
+                                         s->d_status, st));
+        s->p_cur = (s->p_cur + chunks) & 1;
+        sweeps = 0;
+        launches = 1;
+    }
     while (sweeps > 0) {
         const int k = sweeps < per ? sweeps : per;
         const bool last = k == sweeps;
@@ -461,6 +488,11 @@ int natrix_create(int32_t width, int32_t height, natrix_sim** out) {
             e = cudaMalloc(&s->d_marks[i], (size_t)s->marks.words * 4);
             if (e == cudaSuccess) e = cudaMemset(s->d_marks[i], 0, (size_t)s->marks.words * 4);
         }
+    }
+    s->chain_words = jacobi_chain_sync_words(s->maps.config, s->g);
+    if (e == cudaSuccess && s->chain_words > 0) {
+        e = cudaMalloc(&s->d_chain, (size_t)s->chain_words * 4);
+        if (e == cudaSuccess) e = cudaMemset(s->d_chain, 0, (size_t)s->chain_words * 4);
     }
     if (e != cudaSuccess) {
         free_sim(s);
@@ -675,6 +707,10 @@ int natrix_sync(natrix_sim* s, void* stream) {
     NX_CUDA(cudaMemcpy(&status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost));
     if (status) {
         NX_CUDA(cudaMemset(s->d_status, 0, sizeof(int)));
+        if (s->d_chain) {  // a launch that gave up on a wait may have left them uneven
+            NX_CUDA(cudaMemset(s->d_chain, 0, (size_t)s->chain_words * 4));
+            s->chain_claims = s->chain_done = 0;
+        }
         return fail(NATRIX_EDEVICE, "a kernel reported status 0x%x (bounded wait ran out)",
                     status);
     }

@@ -70,6 +70,38 @@ __device__ __forceinline__ bool wait_phase(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
+// Completion counters of persistent kernels whose CTAs wait on each other's
+// items (batch.cu, the sweep chain of jacobi_tma.cu).
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Bounded wait (about 2^24 polls with back-off) for *c >= target.
+__device__ __forceinline__ bool wait_counter(const unsigned long long* c,
+                                             unsigned long long target) {
+    for (int it = 0; it < (1 << 24); ++it) {
+        if (ld_acquire_u64(c) >= target) return true;
+        __nanosleep(64);
+    }
+    return false;
+}
+
+// Order generic-proxy writes (other CTAs' stores released through a
+// completion counter; this CTA's use of the staging memory) before the
+// async-proxy copies the calling thread issues next.
+__device__ __forceinline__ void fence_before_tma() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    fence_proxy_async();
+}
+
 // One tile of work: where to load it from, where to write it, how far to go.
 struct TileJob {
     const CUtensorMap* p;

@@ -55,6 +55,11 @@ struct GridJobs {
     }
 };
 
+// Sweeps per chunk of the sweep chain (its tiles' halo) and the offset of the
+// per-tile counters in its sync block (the claim counter in a line of its own).
+constexpr int kChainSweeps = 8;
+constexpr int kChainDone = 32;
+
 // Most tiles one CTA of a balanced launch takes (kMaxBalancedTiles over the
 // SM count, rounded up, with room to spare).
 constexpr int kMaxCtaTiles = 16;
@@ -231,6 +236,205 @@ __global__ void __launch_bounds__(C::THREADS, 1)
                 issue_tile_loads<C>(smem, bar, jobs(tile_of(k + 1)));
             }
         });
+    }
+}
+
+// ---------------------------------------------------------------------------
+// A step's whole sweep phase in one persistent launch: `chunks` chunks of up
+// to HALO sweeps (the last one may also subtract the gradient), each chunk
+// over every tile, ping-ponging between the two pressure buffers (chunk m
+// reads pbuf[(src0 + m) & 1]).  Items (chunk m, tile) are claimed from a
+// counter in chunk order, the tiles of a chunk with the marked (obstacle)
+// tiles first.  Instead of a launch boundary between chunks, an item of chunk
+// m >= 1 waits until the 3x3 tiles around its own have finished chunk m - 1
+// (one counter of finished chunks per tile): those are the only tiles whose
+// output its region reads (HALO <= the tile size), and the only earlier
+// readers of the output tile it overwrites (the buffer chunk m - 1 read).
+// Dependencies point to items claimed earlier, so the earliest unfinished
+// item can always run, whatever the number of resident CTAs; a CTA counts
+// its finished tile before it waits on anything.
+//
+// Thread 0 claims the next item while the current one's copies land; once
+// the current tile sits in registers it issues the next item's copies into
+// the freed staging buffers, the pressure copy only if the neighbourhood is
+// done (else after the tile, once it is).  After its output stores a tile is
+// released (one fence) and counted.  The counters grow monotonically across
+// launches (the host passes the chunks and claims before the launch); every
+// CTA claims until it draws an index past the list, so a launch adds items +
+// gridDim.x claims.  A wait that runs out (about a second) sets status bit 2
+// and the item runs anyway.
+struct ChainJobs {
+    const JacobiMaps* maps;  // device copy of the grid's maps
+    float* pbuf[2];
+    Grid g;
+    int sweeps, chunks, src0;
+    int tiles_x, tiles_y, n, tx, ty;
+    const uint32_t* slow;  // tile marks of the step (null: tile order)
+    const float2* vin;     // gradient subtraction fused into the last chunk, or null
+    float2* vout;
+    unsigned* sync;  // [0]: claims; [kChainDone + t]: chunks tile t finished
+    unsigned claim_base, done_base;  // claims; chunks every tile finished before the launch
+    __device__ __forceinline__ TileJob job(int chunk, int t) const {
+        const int src = (src0 + chunk) & 1;
+        const int left = sweeps - chunk * kChainSweeps;
+        const bool last = chunk == chunks - 1;
+        return TileJob{&maps->p[src], &maps->div, &maps->flags, pbuf[1 - src], g,
+                       left < kChainSweeps ? left : kChainSweeps, (t % tiles_x) * tx,
+                       (t / tiles_x) * ty, last ? vin : nullptr, last ? vout : nullptr};
+    }
+    // Have the tiles around t finished chunk m - 1?  The nine counters are
+    // read together (relaxed); when they all have, one fence gives the copies
+    // that follow acquire order.
+    __device__ __forceinline__ bool deps_ready(int m, int t) const {
+        if (m == 0) return true;
+        const unsigned target = done_base + (unsigned)m;
+        const int cx = t % tiles_x, cy = t / tiles_x;
+        const int x0 = cx > 0 ? cx - 1 : cx, x1 = cx < tiles_x - 1 ? cx + 1 : cx;
+        const int y0 = cy > 0 ? cy - 1 : cy, y1 = cy < tiles_y - 1 ? cy + 1 : cy;
+        unsigned v[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const int x = min(x0 + k % 3, x1), y = min(y0 + k / 3, y1);
+            v[k] = ld_relaxed_u32(sync + kChainDone + y * tiles_x + x);
+        }
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) ok = ok && (int)(v[k] - target) >= 0;
+        if (ok) asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        return ok;
+    }
+    // bounded wait for deps_ready
+    __device__ __forceinline__ bool wait_deps(int m, int t) const {
+        for (int it = 0; it < (1 << 24); ++it) {
+            if (deps_ready(m, t)) return true;
+            __nanosleep(64);
+        }
+        return false;
+    }
+};
+
+// Tiles of a chunk in claim order: the marked tiles, then the others, each
+// in index order (one warp; n <= kMaxBalancedTiles).
+__device__ void chain_order(const uint32_t* slow, int n, int* order) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int base = lane * 32;
+    const uint32_t valid = base >= n ? 0u : (n - base >= 32 ? FULL : (1u << (n - base)) - 1u);
+    const uint32_t ws = (base < n ? slow[lane] : 0u) & valid;
+    const uint32_t wz = ~ws & valid;
+    int is = __popc(ws), iz = __popc(wz);  // inclusive prefix counts over lanes
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int a = __shfl_up_sync(FULL, is, o), c = __shfl_up_sync(FULL, iz, o);
+        if (lane >= o) {
+            is += a;
+            iz += c;
+        }
+    }
+    const int n_slow = __shfl_sync(FULL, is, 31);
+    int ps = is - __popc(ws), pz = n_slow + iz - __popc(wz);
+    for (uint32_t w = ws; w; w &= w - 1u) order[ps++] = base + __ffs(w) - 1;
+    for (uint32_t w = wz; w; w &= w - 1u) order[pz++] = base + __ffs(w) - 1;
+}
+
+template <class C>
+__global__ void __launch_bounds__(C::THREADS, 1)
+    k_jacobi_chain(const __grid_constant__ ChainJobs J, int* __restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+    __shared__ int s_order[kMaxBalancedTiles];
+    // s_next is set by thread 0 during a tile (after the barrier that starts
+    // it) and read by every thread after the tile
+    __shared__ int s_cur, s_next, s_pending, s_ok;
+    const int tid = threadIdx.x;
+    const int total = J.chunks * J.n;
+    const bool ordered = J.slow != nullptr && J.n <= kMaxBalancedTiles;
+
+    pdl_wait();  // the divergence launch's pressure, divergence, flags and marks
+    if (ordered && tid < 32) chain_order(J.slow, J.n, s_order);
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_barrier_init();
+        s_cur = (int)(atomicAdd(J.sync, 1u) - J.claim_base);
+    }
+    __syncthreads();
+    pdl_trigger();
+    int cur = s_cur;
+    if (cur >= total) return;
+    auto tile_of = [&](int i) {
+        const int q = i % J.n;
+        return ordered ? s_order[q] : q;
+    };
+    if (tid == 0) {
+        const int t = tile_of(cur), m = cur / J.n;
+        const TileJob j = J.job(m, t);
+        issue_static_loads<C>(smem, bar, j);
+        if (!J.wait_deps(m, t)) atomicOr(status, 2);
+        fence_before_tma();
+        issue_pressure_load<C>(smem, bar, j);
+    }
+    for (uint32_t parity = 0;; parity ^= 1u) {
+        const int t = tile_of(cur);
+        const TileJob job = J.job(cur / J.n, t);
+        unsigned claimed = 0;  // thread 0: the next item, in flight during the copy wait
+        if (tid == 0) {
+            claimed = atomicAdd(J.sync, 1u);
+            bool ok = wait_phase(bar, parity);
+            if (!ok) {
+                atomicOr(status, 1);
+                wait_phase(bar, parity);  // let the copies land before the CTA goes on
+            }
+            s_ok = ok ? 1 : 0;
+        }
+        __syncthreads();
+        // a copy that did not land (status bit 1): the tile is skipped but
+        // still counted, so that no other CTA waits for it
+        if (s_ok)
+            rt_tile_body<C>(job, smem, [&] {
+                // staging consumed: prefetch what of the next item is ready
+                // into the freed staging buffers
+                if (tid != 0) return;
+                const int nx = (int)(claimed - J.claim_base);
+                s_next = nx;
+                s_pending = 0;
+                if (nx >= total) return;
+                const int nt = tile_of(nx), nm = nx / J.n;
+                const TileJob nj = J.job(nm, nt);
+                fence_proxy_async();
+                issue_static_loads<C>(smem, bar, nj);
+                if (J.deps_ready(nm, nt)) {
+                    fence_before_tma();
+                    issue_pressure_load<C>(smem, bar, nj);
+                } else {
+                    s_pending = 1;
+                }
+            });
+        else if (tid == 0) {
+            s_next = (int)(claimed - J.claim_base);
+            s_pending = 2;  // nothing issued for it yet
+        }
+        __syncthreads();  // every output store of the tile issued; s_next set
+        if (tid == 0) {
+            // release the tile's stores (ordered before this thread by the
+            // barrier), then count the tile
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+            asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;" ::"l"(J.sync + kChainDone + t)
+                         : "memory");
+        }
+        const int next = s_next;
+        if (next >= total) break;
+        if (tid == 0 && s_pending) {
+            const int t2 = tile_of(next), m2 = next / J.n;
+            const TileJob nj = J.job(m2, t2);
+            if (s_pending == 2) {
+                fence_proxy_async();
+                issue_static_loads<C>(smem, bar, nj);
+            }
+            if (!J.wait_deps(m2, t2)) atomicOr(status, 2);
+            fence_before_tma();
+            issue_pressure_load<C>(smem, bar, nj);
+        }
+        cur = next;
     }
 }
 
@@ -443,6 +647,64 @@ cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbu
     if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st, pdl);
     if (config == JACOBI_RT_C) return launch_rt_jobs<RtC>(jobs, status, st, pdl);
     return launch_tb_jobs<Tb>(jobs, status, st, pdl);
+}
+
+// The chain pays where a chunk has a tile for every SM: measured per step,
+// 2048^2 K80 (304 tiles) 341.9 -> 327.6 us; 256^2 K40 (48 tiles) 40.2 -> 45.2.
+int jacobi_chain_sync_words(int config, Grid g) {
+    if (config == JACOBI_TB) return 0;
+    int tx, ty;
+    jacobi_tile(config, &tx, &ty);
+    const int tiles = ((g.W + tx - 1) / tx) * ((g.H + ty - 1) / ty);
+    return tiles < num_sms() ? 0 : kChainDone + tiles;
+}
+
+template <class C>
+cudaError_t launch_chain(const ChainJobs& jobs, int grid, int* status, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = set_smem(k_jacobi_chain<C>, C::SMEM);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    return launch_kernel(pdl_enabled(), k_jacobi_chain<C>, dim3(grid), dim3(C::THREADS), C::SMEM,
+                         st, jobs, status);
+}
+
+cudaError_t launch_jacobi_chain(const JacobiMaps* d_maps, int config, float* const pbuf[2],
+                                int src, Grid g, int sweeps, const uint32_t* slow,
+                                const float2* vin, float2* vout, unsigned* sync,
+                                unsigned* claims, unsigned* done, bool* fused, int* status,
+                                cudaStream_t st) {
+    static_assert(kChainSweeps == RtA::HALO && kChainSweeps == RtB::HALO &&
+                      kChainSweeps == RtC::HALO,
+                  "a chunk is one tile halo of sweeps");
+    if (config == JACOBI_TB || sweeps < 1) return cudaErrorInvalidValue;
+    int tx, ty;
+    jacobi_tile(config, &tx, &ty);
+    const int tiles_x = (g.W + tx - 1) / tx, tiles_y = (g.H + ty - 1) / ty;
+    const int chunks = (sweeps + kChainSweeps - 1) / kChainSweeps;
+    const int last = sweeps - (chunks - 1) * kChainSweeps;
+    // the fused gradient needs one valid halo cell after the last chunk
+    const bool fuse = vin && last < kChainSweeps;
+    const int n = tiles_x * tiles_y;
+    const int grid = n * chunks < num_sms() ? n * chunks : num_sms();
+    const ChainJobs jobs{d_maps, {pbuf[0], pbuf[1]}, g, sweeps, chunks, src, tiles_x, tiles_y, n,
+                         tx, ty, slow, fuse ? vin : nullptr, fuse ? vout : nullptr, sync,
+                         *claims, *done};
+    cudaError_t e;
+    if (config == JACOBI_RT_A)
+        e = launch_chain<RtA>(jobs, grid, status, st);
+    else if (config == JACOBI_RT_B)
+        e = launch_chain<RtB>(jobs, grid, status, st);
+    else
+        e = launch_chain<RtC>(jobs, grid, status, st);
+    if (e == cudaSuccess) {
+        *claims += (unsigned)(n * chunks + grid);
+        *done += (unsigned)chunks;
+        *fused = fuse;
+    }
+    return e;
 }
 
 cudaError_t launch_jacobi_batch(int config, const JacobiBatchItem* items, int n_items,

@@ -7,7 +7,10 @@ deal, gradient subtraction in its own launch), 1 / 2 / 3 with one register
 tile shape (128x128, 128x144 or 128x32 regions) whatever the grid size;
 NATRIX_SPARSE_FORCING=0 applies a step's velocity ops over the whole grid
 instead of the blocks they reach (with the first op's clamp then done by the
-advection's reads).  Each mode runs in a child
+advection's reads); NATRIX_JACOBI_CHAIN=0 runs a step's sweeps as one launch
+per 8-sweep chunk instead of one persistent launch whose tiles wait on their
+neighbours' previous chunk (used where the grid has a tile for every SM:
+here with the 128x32 tiles, 640 of them).  Each mode runs in a child
 process on the same seeded workload and must reproduce the default run's
 velocity, pressure, divergence, vorticity and density bytes exactly."""
 from __future__ import annotations
@@ -61,6 +64,7 @@ def run_mode(env_extra):
     env.pop("NATRIX_PDL", None)
     env.pop("NATRIX_JACOBI_VARIANT", None)
     env.pop("NATRIX_SPARSE_FORCING", None)
+    env.pop("NATRIX_JACOBI_CHAIN", None)
     env.update(env_extra)
     res = subprocess.run([sys.executable, "-c", SCRIPT, str(ROOT)], env=env,
                          capture_output=True, text=True, timeout=600)
@@ -70,9 +74,12 @@ def run_mode(env_extra):
 
 @pytest.mark.parametrize("env", [{"NATRIX_PDL": "0"}, {"NATRIX_JACOBI_VARIANT": "0"},
                                  {"NATRIX_JACOBI_VARIANT": "1"}, {"NATRIX_JACOBI_VARIANT": "2"},
-                                 {"NATRIX_JACOBI_VARIANT": "3"}, {"NATRIX_SPARSE_FORCING": "0"}],
+                                 {"NATRIX_JACOBI_VARIANT": "3"}, {"NATRIX_SPARSE_FORCING": "0"},
+                                 {"NATRIX_JACOBI_CHAIN": "0"},
+                                 {"NATRIX_JACOBI_CHAIN": "0", "NATRIX_JACOBI_VARIANT": "3"}],
                          ids=["plain-stream-order", "shared-memory-sweeps", "register-tiles-a",
-                              "register-tiles-b", "register-tiles-c", "full-grid-forcing"])
+                              "register-tiles-b", "register-tiles-c", "full-grid-forcing",
+                              "launch-per-chunk", "launch-per-chunk-c"])
 def test_launch_mode_bit_identical(cuda, env):
     base = run_mode({})
     alt = run_mode(env)
