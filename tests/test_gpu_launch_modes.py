@@ -35,10 +35,11 @@ sys.path.insert(0, sys.argv[1])
 from natrix_gb300 import FluidSimulator, SmoothParticlesArea, _lib
 from natrix_gb300 import workloads as wl
 
-W, H = 1056, 1024  # over 1024 forcing blocks: the step lists the blocks its splats reach
+case = json.loads(sys.argv[2])
+W, H = case["W"], case["H"]
 sim = FluidSimulator(W, H)
 den = SmoothParticlesArea(W, H, sim)
-sim.iterations, sim.vorticity, sim.viscosity = 40, 0.35, 0.0
+sim.iterations, sim.vorticity, sim.viscosity = case["K"], case["vort"], case["visc"]
 sim.speed, sim.dissipation = 5.0, 0.99
 den.speed, den.dissipation = 5.0, 0.99
 rng = np.random.default_rng(7)
@@ -59,14 +60,17 @@ print(json.dumps(out))
 """
 
 
-def run_mode(env_extra):
+# over 1024 forcing blocks: the step lists the blocks its splats reach
+DEFAULT = {"W": 1056, "H": 1024, "K": 40, "vort": 0.35, "visc": 0.0}
+
+
+def run_mode(env_extra, case=DEFAULT):
     env = dict(os.environ)
-    env.pop("NATRIX_PDL", None)
-    env.pop("NATRIX_JACOBI_VARIANT", None)
-    env.pop("NATRIX_SPARSE_FORCING", None)
-    env.pop("NATRIX_JACOBI_CHAIN", None)
+    for k in ("NATRIX_PDL", "NATRIX_JACOBI_VARIANT", "NATRIX_SPARSE_FORCING",
+              "NATRIX_JACOBI_CHAIN"):
+        env.pop(k, None)
     env.update(env_extra)
-    res = subprocess.run([sys.executable, "-c", SCRIPT, str(ROOT)], env=env,
+    res = subprocess.run([sys.executable, "-c", SCRIPT, str(ROOT), json.dumps(case)], env=env,
                          capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stderr[-2000:]
     return json.loads(res.stdout.strip().splitlines()[-1])
@@ -83,5 +87,20 @@ def run_mode(env_extra):
 def test_launch_mode_bit_identical(cuda, env):
     base = run_mode({})
     alt = run_mode(env)
+    for k in base:
+        assert alt[k] == base[k], f"{k} differs under {env}"
+
+
+# 1792x1280: 192 tiles of 112x112 (the chain, tiles ordered by the marks) or,
+# forced, 1280 tiles of 112x16 (the chain over more tiles than the marks
+# cover: claimed in index order)
+CHAIN = {"W": 1792, "H": 1280, "K": 40, "vort": 0.35, "visc": 0.0}
+
+
+@pytest.mark.parametrize("env", [{"NATRIX_JACOBI_CHAIN": "0"}, {"NATRIX_JACOBI_VARIANT": "3"}],
+                         ids=["launch-per-chunk", "short-tiles-unordered"])
+def test_sweep_chain_bit_identical(cuda, env):
+    base = run_mode({}, CHAIN)
+    alt = run_mode(env, CHAIN)
     for k in base:
         assert alt[k] == base[k], f"{k} differs under {env}"

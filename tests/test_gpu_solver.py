@@ -328,15 +328,16 @@ def test_residual_regions_many_pockets(cuda, oracle):
     sim.destroy()
 
 
-def test_device_status_reported_and_cleared(cuda, oracle):
+@pytest.mark.parametrize("W,H", [(96, 64), (2048, 2048)])
+def test_device_status_reported_and_cleared(cuda, oracle, W, H):
     """The error path of the kernels' bounded waits, driven from the host: a
     status word written as a sweep whose tile wait ran out would write it
     makes natrix_sync fail once with NATRIX_EDEVICE, the next sync is clean,
     and the handle keeps stepping bit-exact with the oracle (the context stays
-    usable).  Nothing stalls or faults on the GPU."""
+    usable).  At 2048x2048 the sweeps run as the one-launch chain, whose
+    counters the failed sync resets.  Nothing stalls or faults on the GPU."""
     from natrix_gb300 import _lib
 
-    W, H = 96, 64
     sim, den, ref, rden = make_pair(oracle, W, H, iterations=10, vorticity=0.2, speed=5.0,
                                     dissipation=0.99)
     run_workload(sim, den, ref, rden, steps=2, n_splats=3, n_obst=2, seed=3)
