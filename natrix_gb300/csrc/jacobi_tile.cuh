@@ -224,10 +224,13 @@ struct RtCfg {
     static constexpr int OFF_BAR = OFF_X + align128(X_FLOATS * 4);
     static constexpr int SMEM = OFF_BAR + 128;
     static constexpr int THREADS = NW * 32;
+    // resident CTAs per SM: two of 8 warps each, else one
+    static constexpr int CTAS = THREADS <= 256 ? 2 : 1;
     static_assert(TX % 16 == 0, "tile width must keep the uint8 box 16-byte aligned");
     static_assert(RY <= 256 && RXF <= 256, "TMA box dimensions are <= 256");
     static_assert(TY > 0, "region too short for the halo");
     static_assert(SMEM <= 227 * 1024, "shared memory per CTA");
+    static_assert(CTAS == 1 || SMEM + 8 * 1024 <= 113 * 1024, "two CTAs per SM");
 };
 
 // 16 warps x 8 rows: 128x128 region, 112x112 output tile
@@ -239,6 +242,9 @@ using RtB = RtCfg<9, 16, 8>;
 // the rows each warp holds, so more, shorter tiles finish a launch sooner
 // although each recomputes a larger share of halo cells.
 using RtC = RtCfg<2, 16, 8>;
+// 8 warps x 9 rows: 128x72 region, 112x56 output tile, two CTAs per SM, so
+// one CTA's sweep barrier waits are covered by the other's warps.
+using RtD = RtCfg<9, 8, 8>;
 
 // The three copies of a tile on one mbarrier phase: the expected bytes are
 // registered first, so the phase cannot complete before the last copy lands

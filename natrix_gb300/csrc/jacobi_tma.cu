@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(C::THREADS_X* C::THREADS_Y)
 // thread issues the TMA loads of the CTA's next job into the same staging
 // buffers, so the copy overlaps this tile's sweeps.
 template <class C, class Jobs>
-__global__ void __launch_bounds__(C::THREADS, 1)
+__global__ void __launch_bounds__(C::THREADS, C::CTAS)
     k_jacobi_rt(const Jobs jobs, int* __restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
@@ -338,7 +338,7 @@ __device__ void chain_order(const uint32_t* slow, int n, int* order) {
 }
 
 template <class C>
-__global__ void __launch_bounds__(C::THREADS, 1)
+__global__ void __launch_bounds__(C::THREADS, C::CTAS)
     k_jacobi_chain(const __grid_constant__ ChainJobs J, int* __restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
@@ -473,14 +473,15 @@ bool encode_2d(CUtensorMap* map, CUtensorMapDataType dt, int elem_bytes, void* b
 }
 
 // NATRIX_JACOBI_VARIANT forces one tile shape on every single grid (for
-// comparison runs): 0 the shared-memory kernel, 1 / 2 / 3 the register tiles
-// RtA / RtB / RtC (TB on grids at most 96 cells wide, which the register
-// tiles do not serve); otherwise the tile shape is chosen by jacobi_config.
+// comparison runs): 0 the shared-memory kernel, 1 / 2 / 3 / 4 the register
+// tiles RtA / RtB / RtC / RtD (TB on grids at most 96 cells wide, which the
+// register tiles do not serve); otherwise the tile shape is chosen by
+// jacobi_config.
 int forced_variant() {
     static int v = -2;
     if (v == -2) {
         const char* e = getenv("NATRIX_JACOBI_VARIANT");
-        v = (e && e[0] >= '0' && e[0] <= '3' && e[1] == 0) ? e[0] - '0' : -1;
+        v = (e && e[0] >= '0' && e[0] <= '4' && e[1] == 0) ? e[0] - '0' : -1;
     }
     return v;
 }
@@ -520,7 +521,8 @@ cudaError_t launch_rt_jobs(const Jobs& jobs, int* status, cudaStream_t st, bool 
         attr = true;
     }
     if (jobs.n == 0) return cudaSuccess;
-    const int grid = jobs.n < num_sms() ? jobs.n : num_sms();
+    const int slots = num_sms() * C::CTAS;
+    const int grid = jobs.n < slots ? jobs.n : slots;
     return launch_kernel(pdl, k_jacobi_rt<C, Jobs>, dim3(grid), dim3(C::THREADS), C::SMEM, st, jobs,
                          status);
 }
@@ -593,6 +595,8 @@ bool jacobi_tile_marks(int config, Grid g, TileMarks* out) {
         rt_marks<RtB>(g, &m);
     else if (config == JACOBI_RT_C)
         rt_marks<RtC>(g, &m);
+    else if (config == JACOBI_RT_D)
+        rt_marks<RtD>(g, &m);
     else
         return false;
     const long tiles = (long)m.tiles_x * m.tiles_y;
@@ -607,6 +611,7 @@ void jacobi_tile(int config, int* tx, int* ty) {
         case JACOBI_RT_A: *tx = RtA::TX; *ty = RtA::TY; break;
         case JACOBI_RT_B: *tx = RtB::TX; *ty = RtB::TY; break;
         case JACOBI_RT_C: *tx = RtC::TX; *ty = RtC::TY; break;
+        case JACOBI_RT_D: *tx = RtD::TX; *ty = RtD::TY; break;
         default: *tx = Tb::TX; *ty = Tb::TY; break;
     }
 }
@@ -620,6 +625,8 @@ bool jacobi_encode_maps_for(JacobiMaps* maps, int config, float* p0, float* p1, 
         box_of<RtB>(&bx, &by, &bfx);
     else if (config == JACOBI_RT_C)
         box_of<RtC>(&bx, &by, &bfx);
+    else if (config == JACOBI_RT_D)
+        box_of<RtD>(&bx, &by, &bfx);
     else
         box_of<Tb>(&bx, &by, &bfx);
     maps->config = config;
@@ -646,6 +653,7 @@ cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbu
     if (config == JACOBI_RT_A) return launch_rt_jobs<RtA>(jobs, status, st, pdl);
     if (config == JACOBI_RT_B) return launch_rt_jobs<RtB>(jobs, status, st, pdl);
     if (config == JACOBI_RT_C) return launch_rt_jobs<RtC>(jobs, status, st, pdl);
+    if (config == JACOBI_RT_D) return launch_rt_jobs<RtD>(jobs, status, st, pdl);
     return launch_tb_jobs<Tb>(jobs, status, st, pdl);
 }
 
@@ -677,7 +685,7 @@ cudaError_t launch_jacobi_chain(const JacobiMaps* d_maps, int config, float* con
                                 unsigned* claims, unsigned* done, bool* fused, int* status,
                                 cudaStream_t st) {
     static_assert(kChainSweeps == RtA::HALO && kChainSweeps == RtB::HALO &&
-                      kChainSweeps == RtC::HALO,
+                      kChainSweeps == RtC::HALO && kChainSweeps == RtD::HALO,
                   "a chunk is one tile halo of sweeps");
     if (config == JACOBI_TB || sweeps < 1) return cudaErrorInvalidValue;
     int tx, ty;
@@ -688,7 +696,8 @@ cudaError_t launch_jacobi_chain(const JacobiMaps* d_maps, int config, float* con
     // the fused gradient needs one valid halo cell after the last chunk
     const bool fuse = vin && last < kChainSweeps;
     const int n = tiles_x * tiles_y;
-    const int grid = n * chunks < num_sms() ? n * chunks : num_sms();
+    const int slots = num_sms() * (config == JACOBI_RT_D ? RtD::CTAS : 1);
+    const int grid = n * chunks < slots ? n * chunks : slots;
     const ChainJobs jobs{d_maps, {pbuf[0], pbuf[1]}, g, sweeps, chunks, src, tiles_x, tiles_y, n,
                          tx, ty, slow, fuse ? vin : nullptr, fuse ? vout : nullptr, sync,
                          *claims, *done};
@@ -697,8 +706,10 @@ cudaError_t launch_jacobi_chain(const JacobiMaps* d_maps, int config, float* con
         e = launch_chain<RtA>(jobs, grid, status, st);
     else if (config == JACOBI_RT_B)
         e = launch_chain<RtB>(jobs, grid, status, st);
-    else
+    else if (config == JACOBI_RT_C)
         e = launch_chain<RtC>(jobs, grid, status, st);
+    else
+        e = launch_chain<RtD>(jobs, grid, status, st);
     if (e == cudaSuccess) {
         *claims += (unsigned)(n * chunks + grid);
         *done += (unsigned)chunks;

@@ -177,7 +177,13 @@ int wgrad_tc(const uint16_t* dz, int cout, const uint16_t* x0, int c0, const uin
 // ---- Jacobi (jacobi_tma.cu) ------------------------------------------------
 // Jacobi tile kernels: shared-memory sweeps on 64x32 tiles, or register tiled
 // with 112x112 / 112x128 output tiles.
-enum JacobiConfig : int { JACOBI_TB = 0, JACOBI_RT_A = 1, JACOBI_RT_B = 2, JACOBI_RT_C = 3 };
+enum JacobiConfig : int {
+    JACOBI_TB = 0,
+    JACOBI_RT_A = 1,
+    JACOBI_RT_B = 2,
+    JACOBI_RT_C = 3,
+    JACOBI_RT_D = 4
+};
 
 // Tensor maps of one grid for the sweep kernels, encoded for one
 // configuration's boxes.  Kernels read them from device memory (64-byte

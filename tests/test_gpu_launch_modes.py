@@ -3,8 +3,9 @@
 NATRIX_PDL=0 launches the step's kernels in plain stream order instead of
 with programmatic dependent launch; NATRIX_JACOBI_VARIANT=0 runs the sweeps
 with the shared-memory tile kernel on every grid (no register tiles, no tile
-deal, gradient subtraction in its own launch), 1 / 2 / 3 with one register
-tile shape (128x128, 128x144 or 128x32 regions) whatever the grid size;
+deal, gradient subtraction in its own launch), 1 / 2 / 3 / 4 with one
+register tile shape (128x128, 128x144, 128x32, or 128x72 regions on 8-warp
+CTAs two per SM) whatever the grid size;
 NATRIX_SPARSE_FORCING=0 applies a step's velocity ops over the whole grid
 instead of the blocks they reach (with the first op's clamp then done by the
 advection's reads); NATRIX_JACOBI_CHAIN=0 runs a step's sweeps as one launch
@@ -93,12 +94,16 @@ def test_launch_mode_bit_identical(cuda, env):
 
 # 1792x1280: 192 tiles of 112x112 (the chain, tiles ordered by the marks) or,
 # forced, 1280 tiles of 112x16 (the chain over more tiles than the marks
-# cover: claimed in index order)
+# cover: claimed in index order) or 368 tiles of 112x56 (8-warp CTAs, two
+# per SM)
 CHAIN = {"W": 1792, "H": 1280, "K": 40, "vort": 0.35, "visc": 0.0}
 
 
-@pytest.mark.parametrize("env", [{"NATRIX_JACOBI_CHAIN": "0"}, {"NATRIX_JACOBI_VARIANT": "3"}],
-                         ids=["launch-per-chunk", "short-tiles-unordered"])
+@pytest.mark.parametrize("env", [{"NATRIX_JACOBI_CHAIN": "0"}, {"NATRIX_JACOBI_VARIANT": "3"},
+                                 {"NATRIX_JACOBI_VARIANT": "4"},
+                                 {"NATRIX_JACOBI_VARIANT": "4", "NATRIX_JACOBI_CHAIN": "0"}],
+                         ids=["launch-per-chunk", "short-tiles-unordered", "two-ctas-per-sm",
+                              "two-ctas-per-sm-per-chunk"])
 def test_sweep_chain_bit_identical(cuda, env):
     base = run_mode({}, CHAIN)
     alt = run_mode(env, CHAIN)
