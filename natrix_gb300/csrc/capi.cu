@@ -104,11 +104,9 @@ struct natrix_sim {
     TileMarks marks{};             // sweep tiles next to obstacles (geometry; words = 0: off)
     uint32_t* d_marks[2] = {};     // this step's marks / the previous step's
     int marks_cur = 0;
-    // counters of the one-launch sweep phase (launch_jacobi_chain) and their
-    // values after the last such launch
+    // counters of the one-launch sweep phase (launch_jacobi_chain)
     unsigned* d_chain = nullptr;
     int chain_words = 0;
-    unsigned chain_claims = 0, chain_done = 0;
     std::vector<ForceOp> fq;
     std::vector<ShapeOp> sq;
     bool mask_reset_pending = true;  // the mask memory does not hold the current obstacles
@@ -339,8 +337,7 @@ int run_jacobi(natrix_sim* s, int sweeps, cudaStream_t st, const float2* vin = n
         const int chunks = (sweeps + default_sweeps() - 1) / default_sweeps();
         NX_LAUNCH(s, launch_jacobi_chain(s->d_maps, s->maps.config, s->p, s->p_cur, s->g, sweeps,
                                          s->d_marks[s->marks_cur], vin, vout, s->d_chain,
-                                         &s->chain_claims, &s->chain_done, &fuse_last,
-                                         s->d_status, st));
+                                         &fuse_last, s->d_status, st));
         s->p_cur = (s->p_cur + chunks) & 1;
         sweeps = 0;
         launches = 1;
@@ -707,10 +704,8 @@ int natrix_sync(natrix_sim* s, void* stream) {
     NX_CUDA(cudaMemcpy(&status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost));
     if (status) {
         NX_CUDA(cudaMemset(s->d_status, 0, sizeof(int)));
-        if (s->d_chain) {  // a launch that gave up on a wait may have left them uneven
+        if (s->d_chain)  // a sweep launch leaves its counters zeroed; make sure of it
             NX_CUDA(cudaMemset(s->d_chain, 0, (size_t)s->chain_words * 4));
-            s->chain_claims = s->chain_done = 0;
-        }
         return fail(NATRIX_EDEVICE, "a kernel reported status 0x%x (bounded wait ran out)",
                     status);
     }

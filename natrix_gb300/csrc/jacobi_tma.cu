@@ -258,11 +258,11 @@ __global__ void __launch_bounds__(C::THREADS, C::CTAS)
 // the current tile sits in registers it issues the next item's copies into
 // the freed staging buffers, the pressure copy only if the neighbourhood is
 // done (else after the tile, once it is).  After its output stores a tile is
-// released (one fence) and counted.  The counters grow monotonically across
-// launches (the host passes the chunks and claims before the launch); every
-// CTA claims until it draws an index past the list, so a launch adds items +
-// gridDim.x claims.  A wait that runs out (about a second) sets status bit 2
-// and the item runs anyway.
+// released (one fence) and counted.  Every launch starts from zeroed
+// counters: the last CTA to leave (an exit count) zeroes them, when no other
+// CTA touches them any more, so the launch's parameters do not change from
+// step to step and a captured graph replays it correctly.  A wait that runs
+// out (about a second) sets status bit 2 and the item runs anyway.
 struct ChainJobs {
     const JacobiMaps* maps;  // device copy of the grid's maps
     float* pbuf[2];
@@ -272,8 +272,7 @@ struct ChainJobs {
     const uint32_t* slow;  // tile marks of the step (null: tile order)
     const float2* vin;     // gradient subtraction fused into the last chunk, or null
     float2* vout;
-    unsigned* sync;  // [0]: claims; [kChainDone + t]: chunks tile t finished
-    unsigned claim_base, done_base;  // claims; chunks every tile finished before the launch
+    unsigned* sync;  // [0]: claims; [1]: CTAs done; [kChainDone + t]: chunks tile t finished
     __device__ __forceinline__ TileJob job(int chunk, int t) const {
         const int src = (src0 + chunk) & 1;
         const int left = sweeps - chunk * kChainSweeps;
@@ -287,7 +286,7 @@ struct ChainJobs {
     // that follow acquire order.
     __device__ __forceinline__ bool deps_ready(int m, int t) const {
         if (m == 0) return true;
-        const unsigned target = done_base + (unsigned)m;
+        const unsigned target = (unsigned)m;
         const int cx = t % tiles_x, cy = t / tiles_x;
         const int x0 = cx > 0 ? cx - 1 : cx, x1 = cx < tiles_x - 1 ? cx + 1 : cx;
         const int y0 = cy > 0 ? cy - 1 : cy, y1 = cy < tiles_y - 1 ? cy + 1 : cy;
@@ -345,7 +344,7 @@ __global__ void __launch_bounds__(C::THREADS, C::CTAS)
     __shared__ int s_order[kMaxBalancedTiles];
     // s_next is set by thread 0 during a tile (after the barrier that starts
     // it) and read by every thread after the tile
-    __shared__ int s_cur, s_next, s_pending, s_ok;
+    __shared__ int s_cur, s_next, s_pending, s_ok, s_last;
     const int tid = threadIdx.x;
     const int total = J.chunks * J.n;
     const bool ordered = J.slow != nullptr && J.n <= kMaxBalancedTiles;
@@ -355,17 +354,16 @@ __global__ void __launch_bounds__(C::THREADS, C::CTAS)
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_barrier_init();
-        s_cur = (int)(atomicAdd(J.sync, 1u) - J.claim_base);
+        s_cur = (int)atomicAdd(J.sync, 1u);
     }
     __syncthreads();
     pdl_trigger();
     int cur = s_cur;
-    if (cur >= total) return;
     auto tile_of = [&](int i) {
         const int q = i % J.n;
         return ordered ? s_order[q] : q;
     };
-    if (tid == 0) {
+    if (tid == 0 && cur < total) {
         const int t = tile_of(cur), m = cur / J.n;
         const TileJob j = J.job(m, t);
         issue_static_loads<C>(smem, bar, j);
@@ -373,7 +371,7 @@ __global__ void __launch_bounds__(C::THREADS, C::CTAS)
         fence_before_tma();
         issue_pressure_load<C>(smem, bar, j);
     }
-    for (uint32_t parity = 0;; parity ^= 1u) {
+    for (uint32_t parity = 0; cur < total; parity ^= 1u) {
         const int t = tile_of(cur);
         const TileJob job = J.job(cur / J.n, t);
         unsigned claimed = 0;  // thread 0: the next item, in flight during the copy wait
@@ -394,7 +392,7 @@ __global__ void __launch_bounds__(C::THREADS, C::CTAS)
                 // staging consumed: prefetch what of the next item is ready
                 // into the freed staging buffers
                 if (tid != 0) return;
-                const int nx = (int)(claimed - J.claim_base);
+                const int nx = (int)claimed;
                 s_next = nx;
                 s_pending = 0;
                 if (nx >= total) return;
@@ -410,7 +408,7 @@ __global__ void __launch_bounds__(C::THREADS, C::CTAS)
                 }
             });
         else if (tid == 0) {
-            s_next = (int)(claimed - J.claim_base);
+            s_next = (int)claimed;
             s_pending = 2;  // nothing issued for it yet
         }
         __syncthreads();  // every output store of the tile issued; s_next set
@@ -422,8 +420,7 @@ __global__ void __launch_bounds__(C::THREADS, C::CTAS)
                          : "memory");
         }
         const int next = s_next;
-        if (next >= total) break;
-        if (tid == 0 && s_pending) {
+        if (next < total && tid == 0 && s_pending) {
             const int t2 = tile_of(next), m2 = next / J.n;
             const TileJob nj = J.job(m2, t2);
             if (s_pending == 2) {
@@ -436,6 +433,17 @@ __global__ void __launch_bounds__(C::THREADS, C::CTAS)
         }
         cur = next;
     }
+    // Leave: this CTA's claims and counts are done (its last count and its
+    // claim past the list come before the fence); the last CTA out zeroes
+    // the counters for the next launch.
+    if (tid == 0) {
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        s_last = atomicAdd(J.sync + 1, 1u) == gridDim.x - 1 ? 1 : 0;
+        if (s_last) asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    }
+    __syncthreads();
+    if (s_last)
+        for (int i = tid; i < kChainDone + J.n; i += C::THREADS) J.sync[i] = 0u;
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
@@ -681,9 +689,8 @@ cudaError_t launch_chain(const ChainJobs& jobs, int grid, int* status, cudaStrea
 
 cudaError_t launch_jacobi_chain(const JacobiMaps* d_maps, int config, float* const pbuf[2],
                                 int src, Grid g, int sweeps, const uint32_t* slow,
-                                const float2* vin, float2* vout, unsigned* sync,
-                                unsigned* claims, unsigned* done, bool* fused, int* status,
-                                cudaStream_t st) {
+                                const float2* vin, float2* vout, unsigned* sync, bool* fused,
+                                int* status, cudaStream_t st) {
     static_assert(kChainSweeps == RtA::HALO && kChainSweeps == RtB::HALO &&
                       kChainSweeps == RtC::HALO && kChainSweeps == RtD::HALO,
                   "a chunk is one tile halo of sweeps");
@@ -699,8 +706,7 @@ cudaError_t launch_jacobi_chain(const JacobiMaps* d_maps, int config, float* con
     const int slots = num_sms() * (config == JACOBI_RT_D ? RtD::CTAS : 1);
     const int grid = n * chunks < slots ? n * chunks : slots;
     const ChainJobs jobs{d_maps, {pbuf[0], pbuf[1]}, g, sweeps, chunks, src, tiles_x, tiles_y, n,
-                         tx, ty, slow, fuse ? vin : nullptr, fuse ? vout : nullptr, sync,
-                         *claims, *done};
+                         tx, ty, slow, fuse ? vin : nullptr, fuse ? vout : nullptr, sync};
     cudaError_t e;
     if (config == JACOBI_RT_A)
         e = launch_chain<RtA>(jobs, grid, status, st);
@@ -710,11 +716,7 @@ cudaError_t launch_jacobi_chain(const JacobiMaps* d_maps, int config, float* con
         e = launch_chain<RtC>(jobs, grid, status, st);
     else
         e = launch_chain<RtD>(jobs, grid, status, st);
-    if (e == cudaSuccess) {
-        *claims += (unsigned)(n * chunks + grid);
-        *done += (unsigned)chunks;
-        *fused = fuse;
-    }
+    if (e == cudaSuccess) *fused = fuse;
     return e;
 }
 

@@ -236,16 +236,16 @@ cudaError_t launch_jacobi(const JacobiMaps* d_maps, int config, float* const pbu
 // the last chunk's result in pbuf[(src + chunks) & 1]; vin / vout as for
 // launch_jacobi, fused into the last chunk when it has fewer sweeps than the
 // halo (*fused says whether it was).  `sync` (device, jacobi_chain_sync_words
-// words, zeroed once) holds the counters the launch's CTAs wait on; *claims
-// and *done are their host-side values, advanced by the launch.
+// words, zeroed once) holds the counters the launch's CTAs wait on; the
+// launch leaves them zeroed, so its parameters are the same every step (a
+// captured graph replays it).
 // jacobi_chain_sync_words is 0 where the chain does not pay (fewer tiles than
 // SMs) or cannot run (the shared-memory configuration).
 int jacobi_chain_sync_words(int config, Grid g);
 cudaError_t launch_jacobi_chain(const JacobiMaps* d_maps, int config, float* const pbuf[2],
                                 int src, Grid g, int sweeps, const uint32_t* slow,
-                                const float2* vin, float2* vout, unsigned* sync,
-                                unsigned* claims, unsigned* done, bool* fused, int* status,
-                                cudaStream_t st);
+                                const float2* vin, float2* vout, unsigned* sync, bool* fused,
+                                int* status, cudaStream_t st);
 // One batched launch: every item is one tile of one simulation (device arrays).
 cudaError_t launch_jacobi_batch(int config, const JacobiBatchItem* items, int n_items,
                                 const JacobiBatchSim* sims, int* status, cudaStream_t st);
