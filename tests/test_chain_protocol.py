@@ -15,7 +15,11 @@ grids of 1 to 6 tiles a side) must:
     or newer;
   * overwrite a tile of a buffer only after every item that reads the old
     contents there has read them;
-  * finish (the earliest unfinished item can always run).
+  * finish (the earliest unfinished item can always run);
+  * zero the counters only after every claim and count of the launch: each
+    CTA adds itself to an exit count after its claim past the list and its
+    last count, and the last one out resets the counters for the next
+    launch.
 A single summed counter per tile (the neighbourhood's completions added up)
 is also modelled and shown to admit a schedule that reads a stale tile, the
 reason the kernel keeps one counter per tile."""
@@ -46,15 +50,16 @@ def simulate(tx, ty, chunks, ctas, rng, summed=False):
         for u in hood(t, tx, ty):
             pending_reads[0][u].add((0, t))
     claim = 0
+    exits = 0
+    reset = False
     # CTA state: [current item or None, phase, remaining work, next claimed item]
     state = []
     for _ in range(ctas):
         if claim < total:
             state.append([claim, "wait", 0, None])
-            claim += 1
         else:
-            state.append([None, "idle", 0, None])
-            claim += 1
+            state.append([None, "exit", 0, None])  # drew past the list: leaves
+        claim += 1
 
     def ready(i):
         m, t = divmod(i, n)
@@ -66,16 +71,27 @@ def simulate(tx, ty, chunks, ctas, rng, summed=False):
 
     finished = 0
     steps = 0
-    while finished < total:
+    while finished < total or any(s[1] == "exit" for s in state):
         steps += 1
         if steps > 200000:
             return "no progress"
         movable = [c for c, s in enumerate(state)
-                   if s[1] == "run" or (s[1] == "wait" and ready(s[0]))]
+                   if s[1] in ("run", "exit") or (s[1] == "wait" and ready(s[0]))]
         if not movable:
             return "deadlock"
         c = rng.choice(movable)
         s = state[c]
+        if s[1] == "exit":
+            # the exit count; the last CTA out zeroes the counters
+            if reset:
+                return "a CTA left after the counters were reset"
+            exits += 1
+            state[c] = [None, "gone", 0, None]
+            if exits == ctas:
+                reset = True
+            continue
+        if reset:
+            return "counters used after the reset"
         i = s[0]
         m, t = divmod(i, n)
         src = m & 1
@@ -110,7 +126,9 @@ def simulate(tx, ty, chunks, ctas, rng, summed=False):
             if s[3] is not None and s[3] < total:
                 state[c] = [s[3], "wait", 0, None]
             else:
-                state[c] = [None, "idle", 0, None]
+                state[c] = [None, "exit", 0, None]
+    if not reset:
+        return "counters never reset"
     return None
 
 
