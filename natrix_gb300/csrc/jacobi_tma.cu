@@ -21,6 +21,10 @@
 //     while the current one sweeps (grids wider than ~100 cells);
 //   * k_jacobi_tb: shared-memory sweeps on a shrinking region, one tile per
 //     CTA, several CTAs per SM (narrow grids).
+// A third, k_jacobi_chain, runs every chunk of HALO sweeps of a step in one
+// persistent launch on grids with a register tile for every SM: tiles wait
+// for their neighbours' previous chunk instead of a launch boundary (see the
+// comment above it).
 // Every mbarrier wait is bounded; on time-out the kernel records status bit 1,
 // waits once more (bounded) for its copies, and returns without writing.
 #include <cudaTypedefs.h>
