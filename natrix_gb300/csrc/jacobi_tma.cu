@@ -26,7 +26,8 @@
 // for their neighbours' previous chunk instead of a launch boundary (see the
 // comment above it).
 // Every mbarrier wait is bounded; on time-out the kernel records status bit 1,
-// waits once more (bounded) for its copies, and returns without writing.
+// waits once more (bounded) for its copies, and returns without writing (the
+// chain instead skips that tile and still counts it, so no CTA waits on it).
 #include <cudaTypedefs.h>
 
 #include <cstdlib>
